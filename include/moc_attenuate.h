@@ -1,0 +1,191 @@
+/*
+ * moc_attenuate.h — C ABI of the GB300 segment-attenuation sweep (libmocatt.so).
+ *
+ * What it replaces in the reference (ANL-CESAR/SimpleMOC-kernel):
+ *   - void run_kernel(Input*, Source*, Table*)            src/cpu/SimpleMOC-kernel_header.h:81
+ *       the OpenMP loop over segments, src/cpu/kernel.c:3-73, called once from
+ *       src/cpu/main.c:46                                  -> moc_attenuate_fwd[_host]
+ *   - void attenuate_segment(Input*, Source*, int QSR_id, int FAI_id, float* state_flux,
+ *       SIMD_Vectors*, Table*)                             src/cpu/SimpleMOC-kernel_header.h:82-84
+ *       the per-segment body, src/cpu/kernel.c:75-333      -> one (segment, group) lane of
+ *                                                             the device sweep
+ *   - __global__ run_kernel(Input, Source*, Source_Arrays, Table*, curandState*, float*, int)
+ *                                                          src/cuda/SimpleMOC-kernel_header.h:66-68
+ *   - Table* buildExponentialTable(float precision, float maxVal, Input*)
+ *                                                          src/cpu/init.c:81-117
+ *                                                          -> moc_build_exp_table
+ *   - float interpolateTable(Table*, float x)              src/cpu/kernel.c:337-361
+ *                                                          -> MOC_EXP_TABLE mode
+ *
+ * Differences in meaning, all deliberate:
+ *   - Segments are explicit inputs (region, interval, ds per segment, grouped by track
+ *     in CSR order) instead of rand_r draws inside the loop (src/cpu/kernel.c:47-50);
+ *     ds is per segment instead of the constant 0.7f (src/cpu/kernel.c:104).
+ *   - psi is carried per track (psi[T][G]) instead of per OpenMP thread
+ *     (src/cpu/kernel.c:24-30).
+ *   - The tally fine_flux[r][i][g] += weight * flux_integral is an atomic reduction on
+ *     the device instead of a per-(region, interval) omp_lock (src/cpu/kernel.c:265-281).
+ *   - Errors come back as moc_status_t; nothing exits (the reference has no error path).
+ *
+ * Conventions:
+ *   - Every pointer in moc_problem_t is caller-owned device memory (moc_attenuate_fwd)
+ *     or host memory (moc_attenuate_fwd_host); the library never frees them.
+ *   - Float arrays must be 16-byte aligned and group_stride a multiple of 4, so each
+ *     row is read as 128-bit vectors.
+ *   - Device calls are asynchronous and ordered on `stream` (a cudaStream_t passed as
+ *     void*; NULL = legacy default stream). A handle serves one host thread at a time;
+ *     distinct handles are independent.
+ */
+#ifndef MOC_ATTENUATE_H
+#define MOC_ATTENUATE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MOC_ABI_VERSION 1
+
+typedef enum {
+    MOC_OK = 0,
+    MOC_ERR_INVALID_ARG = 1,     /* NULL pointer, negative size, unknown enum value   */
+    MOC_ERR_MISALIGNED = 2,      /* a float array is not 16-byte aligned             */
+    MOC_ERR_UNSUPPORTED = 3,     /* valid but unsupported combination                */
+    MOC_ERR_CUDA = 4,            /* a CUDA runtime call failed (see moc_last_error)   */
+    MOC_ERR_NO_DEVICE = 5,       /* no CUDA device, or the device index is invalid   */
+    MOC_ERR_OUT_OF_MEMORY = 6,   /* workspace allocation failed                      */
+    MOC_ERR_BAD_INDEX = 7,       /* checked mode: a segment named a region, interval
+                                    or track offset out of range; nothing was added  */
+    MOC_ERR_DEVICE_TIMEOUT = 8   /* a bounded device-side wait gave up               */
+} moc_status_t;
+
+typedef struct moc_handle_s *moc_handle_t;
+
+/* Exponential evaluation: 1 - exp(-tau). */
+typedef enum {
+    MOC_EXP_FULL = 0,   /* range-reduced exp (the reference's 1.f - expf(-tau),
+                           src/cpu/kernel.c:221)                                        */
+    MOC_EXP_TABLE = 1   /* the reference's piecewise-linear table, built by
+                           src/cpu/init.c:81-117 and read by src/cpu/kernel.c:337-361,
+                           reproduced exactly (including its slope sign and index rule)   */
+} moc_exp_mode_t;
+
+/* Storage precision of sigT and the axial source coefficients (math is always FP32). */
+typedef enum {
+    MOC_PREC_FP32 = 0,  /* plain method: the reference computation in FP32 (drop-in)     */
+    MOC_PREC_BF16 = 1,  /* precision form: bf16 storage, stable small-tau math           */
+    MOC_PREC_FP16 = 2   /* precision form: fp16 storage, stable small-tau math           */
+} moc_precision_t;
+
+/* How fine_flux tallies are accumulated. */
+typedef enum {
+    MOC_TALLY_ATOMIC_FP32 = 0,  /* vector red.global.add.f32 into fine_flux             */
+    MOC_TALLY_COMPENSATED = 1,  /* FP32 atomics with an error-free-transform companion
+                                   array (hi + lo), combined in FP64 at the end         */
+    MOC_TALLY_FP64 = 2          /* FP64 atomics into a workspace, added at the end       */
+} moc_tally_t;
+
+/*
+ * One sweep problem. Sizes follow the reference's Input (src/cpu/SimpleMOC-kernel_header.h:
+ * 24-42): n_regions = source_3D_regions, n_intervals = fine_axial_intervals,
+ * n_groups = egroups, n_segments = segments. Arrays follow Source
+ * (src/cpu/SimpleMOC-kernel_header.h:45-52): fine_source, fine_flux and sigT, one
+ * contiguous array each.
+ */
+typedef struct {
+    int32_t n_regions;            /* R >= 1                                              */
+    int32_t n_intervals;          /* I, 2..255                                           */
+    int32_t n_groups;             /* G >= 1                                              */
+    int32_t group_stride;         /* row stride in floats, >= G, multiple of 4          */
+    int32_t n_tracks;             /* T >= 0                                              */
+    int32_t reserved0;
+    int64_t n_segments;           /* S >= 0                                              */
+    const int64_t *track_offsets; /* [T+1], nondecreasing, track_offsets[0] = 0,
+                                     track_offsets[T] = S                                */
+    const int32_t *seg_region;    /* [S] region of each segment, in [0, R)               */
+    const uint8_t *seg_interval;  /* [S] fine axial interval, in [0, I)                  */
+    const float *seg_ds;          /* [S] segment length, >= 0                            */
+    const float *sigT;            /* [R][group_stride] total cross section, > 0          */
+    const float *source;          /* [R][I][group_stride] fine source                    */
+    float *fine_flux;             /* [R][I][group_stride] tallies are ADDED here         */
+    float *psi;                   /* [T][group_stride] in: incoming, out: outgoing flux  */
+} moc_problem_t;
+
+typedef struct {
+    moc_exp_mode_t exp_mode;
+    int32_t table_points;         /* N of the table (reference: 353), >= 2              */
+    float table_max;              /* maxVal of the table (reference: 10.0f)              */
+    moc_precision_t precision;
+    moc_tally_t tally;
+    /* Placeholder constants of src/cpu/kernel.c:99-103 (defaults are the reference's). */
+    float dz, zin, weight, mu, mu2;
+    int32_t checked;              /* 1: bounds-check every segment first (an extra pass)
+                                     and return MOC_ERR_BAD_INDEX without touching
+                                     fine_flux or psi                                     */
+    int32_t vec;                  /* groups per lane: 0 = auto, else 1, 2 or 4          */
+    int32_t warps_per_block;      /* 0 = auto, else 1..32                               */
+    int32_t reserved[4];
+} moc_fwd_opts_t;
+
+/* Reference defaults: FULL exp, N=353 / maxVal=10 table, FP32, atomic tallies,
+ * dz=0.1 zin=0.3 weight=0.5 mu=0.9 mu2=0.3. */
+void moc_fwd_opts_default(moc_fwd_opts_t *opts);
+
+/* Create a handle on CUDA device `device` (it becomes current for the handle's calls). */
+moc_status_t moc_create(moc_handle_t *handle, int device);
+/* Destroy a handle and free its workspace (synchronises its device). NULL is a no-op. */
+moc_status_t moc_destroy(moc_handle_t handle);
+
+/*
+ * Attenuate every segment of every track, in track order, on device buffers.
+ * For each track t and each segment j of it (in CSR order) and each group g:
+ *   fine_flux[region_j][interval_j][g] += weight * flux_integral(psi[t][g])
+ *   psi[t][g] = attenuated psi                       (src/cpu/kernel.c:111-332)
+ * Asynchronous on `stream`; returns after enqueueing (checked mode waits for the
+ * index check). The handle's workspace (axial coefficients, table) is reused by
+ * later calls, so calls on one handle must not overlap on different streams.
+ */
+moc_status_t moc_attenuate_fwd(moc_handle_t handle, const moc_problem_t *problem,
+                               const moc_fwd_opts_t *opts, void *stream);
+
+/*
+ * Same sweep, with every pointer of `problem` in HOST memory: the call copies the
+ * inputs to device memory held by the handle, sweeps, copies psi and fine_flux back,
+ * and returns when the host arrays hold the results. This is the drop-in for a host
+ * program that calls run_kernel(I, S, table) on host arrays (src/cpu/main.c:46).
+ * Page-locked host memory makes the copies faster but is not required.
+ */
+moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *problem,
+                                    const moc_fwd_opts_t *opts);
+
+/*
+ * Wait for `stream`, then report and clear the device-side error word of the handle:
+ * MOC_ERR_BAD_INDEX if any sweep since the last call met a segment whose region or
+ * interval was out of range, or a track whose offsets were not inside [0, S]. Such a
+ * segment or track is skipped by the sweep (nothing is read or written through its
+ * indices); the rest of the sweep completes.
+ */
+moc_status_t moc_synchronize(moc_handle_t handle, void *stream);
+
+/*
+ * Build the reference's exponential table on the host (src/cpu/init.c:81-117) for a
+ * given point count N: dx = maxVal / N, values[2n] = -exp(-n dx),
+ * values[2n+1] = 1 + (n dx - 1) exp(-n dx), and the lookup bound maxVal - dx.
+ * values has room for 2N floats. The reference picks N from a precision
+ * (N = (int)(maxVal * sqrt(1 / (8 * precision * 0.01))), 353 for 0.01 / 10.0).
+ */
+moc_status_t moc_build_exp_table(int32_t n_points, float max_val, float *values,
+                                 float *dx, float *lookup_max);
+
+/* Static description of a status code. */
+const char *moc_status_string(moc_status_t status);
+/* Text of the last CUDA error recorded by this handle ("" if none). */
+const char *moc_last_error(moc_handle_t handle);
+/* MOC_ABI_VERSION of the loaded library. */
+int32_t moc_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOC_ATTENUATE_H */

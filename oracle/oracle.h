@@ -1,0 +1,81 @@
+/*
+ * oracle.h — CPU oracle for the segment-attenuation sweep.
+ *
+ * TEST INFRASTRUCTURE ONLY. Nothing in the product (libmocatt.so, its Python wrapper)
+ * links, loads or calls this code. Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg use it, and only as the checker or the timed CPU reference arm.
+ *
+ * Pinning: oracle_fwd_fp32 is checked bit for bit against the reference's own
+ * attenuate_segment (src/cpu/kernel.c:75-333), compiled unmodified from the reference
+ * sources by oracle/Makefile into oracle/_ref/ (tests/test_oracle_pin.py). The golden
+ * fixtures under tests/golden/ were produced by that pinned pair.
+ *
+ * Problem and option structs are the library's (moc_attenuate.h); here every pointer
+ * is host memory.
+ */
+#ifndef MOC_ORACLE_H
+#define MOC_ORACLE_H
+
+#include <stdint.h>
+#include "moc_attenuate.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Exponential table, restating buildExponentialTable (src/cpu/init.c:81-117) for a
+ * given N: values[2N], dx, and the lookup bound maxVal - dx. */
+void oracle_build_table(int32_t n_points, float max_val, float *values, float *dx,
+                        float *lookup_max);
+/* Table lookup, restating interpolateTable (src/cpu/kernel.c:337-361). */
+float oracle_table_lookup(const float *values, float dx, float lookup_max, float x);
+
+/* FP32 restatement of attenuate_segment (src/cpu/kernel.c:99-332), swept over tracks
+ * in CSR order, one track after another (deterministic). Updates p->psi and
+ * p->fine_flux in place. Returns 0, or -1 on invalid input. */
+int oracle_fwd_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o);
+
+/* Same arithmetic, OpenMP over tracks with one omp_lock per (region, interval) around
+ * the tally, as src/cpu/kernel.c:265-281. Tally order varies between runs. This is the
+ * timed CPU reference arm. nthreads <= 0 uses all available threads. */
+int oracle_fwd_fp32_omp(const moc_problem_t *p, const moc_fwd_opts_t *o, int nthreads);
+
+/*
+ * FP64 oracle of the same formula on the same FP32 inputs and FP32 constants, with
+ * the cancelling small-tau terms (tau - e and tau(tau(tau-3)+6) - 6e, e = 1-exp(-tau))
+ * evaluated by their Taylor series. Outputs (all [.][group_stride]):
+ *   psi_out   outgoing psi per track          ff_out  fine_flux (initial + tallies)
+ *   a_psi     error-magnitude companion of psi_out
+ *   a_ff      error-magnitude companion of ff_out (|initial| + sum of tally companions)
+ *   abs_tally sum of |tally| per fine_flux entry
+ *   hits      [R*I] number of segments that tallied into each (region, interval)
+ * The companion A bounds the rounding error of an FP32 evaluation of the reference
+ * formula: |x_fp32 - x| <= c * 2^-24 * A for a small operation count c (tally sums add
+ * hits * 2^-24 * abs_tally). Any output pointer may be NULL. nthreads <= 0: all.
+ */
+int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi_out,
+                    double *ff_out, double *a_psi, double *a_ff, double *abs_tally,
+                    int64_t *hits, int nthreads);
+
+/*
+ * FP64 adjoint of the sweep for L = sum w . fine_flux_out + sum v . psi_out
+ * (w [R][I][group_stride], v [T][group_stride]). Outputs dL/dsigT [R][group_stride],
+ * dL/dsource [R][I][group_stride], dL/dpsi_in [T][group_stride] (overwritten).
+ * Hand-derived reverse sweep over each track; exp terms as in oracle_fwd_fp64.
+ */
+int oracle_adj_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, const double *w,
+                    const double *v, double *d_sigT, double *d_source, double *d_psi_in,
+                    int nthreads);
+
+/* FP64 forward loss only (for central differences): returns L for the given inputs,
+ * with sigT/source/psi_in taken in double precision from the arrays given. Groups are
+ * independent, so group >= 0 returns the part of L carried by that group alone (a
+ * parameter of group g moves only that part); group < 0 returns all of L. */
+double oracle_loss_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o,
+                        const double *sigT, const double *source, const double *psi_in,
+                        const double *w, const double *v, int32_t group);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

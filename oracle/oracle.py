@@ -1,0 +1,173 @@
+"""ctypes bindings of the CPU oracle (oracle/oracle.h) and of the pinned reference.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg, as the checker or the timed CPU reference arm. The product never
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "simplemoc-kernel_gb300"))
+import mocatt  # noqa: E402  (struct definitions and the input generator)
+
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+CPU_BENCH = os.path.join(HERE, "_build", "cpu_bench")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_P = C.c_void_p
+_PP = C.POINTER(mocatt.MocProblem)
+_PO = C.POINTER(mocatt.MocFwdOpts)
+_SIGS = {
+    "oracle_build_table": (None, [C.c_int32, C.c_float, _P, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+    "oracle_table_lookup": (C.c_float, [_P, C.c_float, C.c_float, C.c_float]),
+    "oracle_fwd_fp32": (C.c_int, [_PP, _PO]),
+    "oracle_fwd_fp32_omp": (C.c_int, [_PP, _PO, C.c_int]),
+    "oracle_fwd_fp64": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, _P, C.c_int]),
+    "oracle_adj_fp64": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, C.c_int]),
+    "oracle_loss_fp64": (C.c_double, [_PP, _PO, _P, _P, _P, _P, _P, C.c_int32]),
+}
+
+_lib = None
+
+
+def build(reference_root: str | None = None) -> None:
+    """make -C oracle (and the pinned reference when its sources are given)."""
+    cmd = ["make", "-s", "-C", HERE, "all"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    if reference_root and os.path.isdir(os.path.join(reference_root, "src", "cpu")):
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"],
+                           capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"reference pin build failed:\n{r.stdout}\n{r.stderr}")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        for n, (res, args) in _SIGS.items():
+            f = getattr(_lib, n)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def table(n_points: int, max_val: float):
+    vals = np.zeros(2 * n_points, np.float32)
+    dx, lk = C.c_float(), C.c_float()
+    lib().oracle_build_table(n_points, max_val, vals.ctypes.data, C.byref(dx), C.byref(lk))
+    return vals, dx.value, lk.value
+
+
+def fwd_fp32(hp: "mocatt.HostProblem", opts=None, threads: int | None = None):
+    """Restated reference sweep in FP32 on a copy; returns (psi, fine_flux). threads=None
+    runs the deterministic sequential sweep, else the OpenMP/lock version."""
+    opts = opts or mocatt.default_opts()
+    q = hp.copy()
+    prob = q.c_struct()
+    if threads is None:
+        rc = lib().oracle_fwd_fp32(C.byref(prob), C.byref(opts))
+    else:
+        rc = lib().oracle_fwd_fp32_omp(C.byref(prob), C.byref(opts), threads)
+    if rc:
+        raise ValueError("oracle rejected the problem")
+    return q.psi, q.fine_flux
+
+
+def fwd_fp64(hp: "mocatt.HostProblem", opts=None, threads: int = 0) -> dict:
+    """FP64 oracle with error-magnitude companions (see oracle.h)."""
+    opts = opts or mocatt.default_opts()
+    prob = hp.c_struct()
+    ncell = hp.R * hp.I
+    out = {k: np.zeros(shape, np.float64) for k, shape in (
+        ("psi", (hp.T, hp.Gs)), ("ff", (ncell, hp.Gs)), ("a_psi", (hp.T, hp.Gs)),
+        ("a_ff", (ncell, hp.Gs)), ("abs_tally", (ncell, hp.Gs)))}
+    out["hits"] = np.zeros(ncell, np.int64)
+    rc = lib().oracle_fwd_fp64(C.byref(prob), C.byref(opts), out["psi"].ctypes.data,
+                               out["ff"].ctypes.data, out["a_psi"].ctypes.data,
+                               out["a_ff"].ctypes.data, out["abs_tally"].ctypes.data,
+                               out["hits"].ctypes.data, threads)
+    if rc:
+        raise ValueError("oracle rejected the problem")
+    return out
+
+
+def adj_fp64(hp, w, v, opts=None, threads: int = 0) -> dict:
+    opts = opts or mocatt.default_opts()
+    prob = hp.c_struct()
+    w = np.ascontiguousarray(w, np.float64)
+    v = np.ascontiguousarray(v, np.float64)
+    out = {"d_sigT": np.zeros((hp.R, hp.Gs)), "d_source": np.zeros((hp.R * hp.I, hp.Gs)),
+           "d_psi_in": np.zeros((hp.T, hp.Gs))}
+    rc = lib().oracle_adj_fp64(C.byref(prob), C.byref(opts), w.ctypes.data, v.ctypes.data,
+                               out["d_sigT"].ctypes.data, out["d_source"].ctypes.data,
+                               out["d_psi_in"].ctypes.data, threads)
+    if rc:
+        raise ValueError("oracle rejected the problem")
+    return out
+
+
+def loss_fp64(hp, sigT, source, psi_in, w, v, group: int = -1, opts=None) -> float:
+    opts = opts or mocatt.default_opts()
+    prob = hp.c_struct()
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (sigT, source, psi_in, w, v)]
+    return lib().oracle_loss_fp64(C.byref(prob), C.byref(opts),
+                                  *[a.ctypes.data for a in arrs], group)
+
+
+# ------------------------------------------------------------------------------------
+# The pinned reference (oracle/_ref, built only where the reference sources exist)
+# ------------------------------------------------------------------------------------
+def pinref_available() -> bool:
+    return all(os.path.exists(os.path.join(REF_DIR, f))
+               for f in ("libpinref.so", "libpinref_table.so"))
+
+
+def _pinlib(table_mode: bool):
+    name = "libpinref_table.so" if table_mode else "libpinref.so"
+    lib_ = C.CDLL(os.path.join(REF_DIR, name))
+    lib_.pinref_sweep.restype = C.c_int
+    lib_.pinref_sweep.argtypes = [_PP, _P, C.c_int32, C.c_float, C.c_float]
+    lib_.pinref_build_table.restype = C.c_int
+    lib_.pinref_build_table.argtypes = [C.c_float, C.c_float, _P, C.c_int32,
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float)]
+    return lib_
+
+
+def pinref_table(precision: float, max_val: float):
+    """The reference's own buildExponentialTable(precision, maxVal)."""
+    cap = 1 << 22
+    vals = np.zeros(cap, np.float32)
+    n, dx, lk = C.c_int32(), C.c_float(), C.c_float()
+    if _pinlib(False).pinref_build_table(precision, max_val, vals.ctypes.data, cap,
+                                         C.byref(n), C.byref(dx), C.byref(lk)):
+        raise ValueError("table too large")
+    return vals[:2 * n.value].copy(), n.value, dx.value, lk.value
+
+
+def pinref_sweep(hp, table_values=None, table_dx=0.0, table_lookup=0.0):
+    """The reference's attenuate_segment over every track (ds fixed at 0.7 by the
+    reference); returns (psi, fine_flux) of a copy."""
+    q = hp.copy()
+    prob = q.c_struct()
+    tm = table_values is not None
+    tv = np.ascontiguousarray(table_values, np.float32) if tm else None
+    rc = _pinlib(tm).pinref_sweep(C.byref(prob), tv.ctypes.data if tm else None,
+                                  len(tv) // 2 if tm else 0, table_dx, table_lookup)
+    if rc:
+        raise ValueError("pinref rejected the problem")
+    return q.psi, q.fine_flux

@@ -1,0 +1,98 @@
+"""In-tree build of the native libraries (nvcc + gcc, no cmake, no setup.py).
+
+    libmocatt.so    the C-ABI sweep library (include/moc_attenuate.h), CUDA for sm_103a
+    libmocsynth.so  the seeded input generator (include/moc_synth.h), plain C
+
+Objects are rebuilt only when a source or header is newer. Translation units compile in
+parallel. Host code is compiled with -ffp-contract=off so it rounds identically on x86
+and Arm.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+HOST = os.path.join(PKG, "host")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + [
+    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+    "-I" + INCLUDE, "-I" + CSRC,
+]
+CU_SOURCES = ["moc_api.cu", "moc_sweep.cu"]
+
+LIB = os.path.join(BUILD, "libmocatt.so")
+SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libmocatt.so")
+
+
+def _headers() -> list[str]:
+    out = []
+    for d in (CSRC, INCLUDE):
+        out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh"))]
+    return out
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd: list[str], verbose: bool) -> None:
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed ({r.returncode}): {' '.join(cmd)}\n"
+                           f"{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout + r.stderr, flush=True)
+
+
+def build(verbose: bool = False) -> dict:
+    """Build both libraries; returns their paths."""
+    os.makedirs(BUILD, exist_ok=True)
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + hdrs):
+            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+    synth_src = os.path.join(HOST, "synth.c")
+    synth_cmd = None
+    if _stale(SYNTH_LIB, [synth_src, os.path.join(INCLUDE, "moc_synth.h")]):
+        synth_cmd = ["gcc", "-std=gnu99", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                     "-I" + INCLUDE, synth_src, "-o", SYNTH_LIB, "-lm"]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs) + 1)) as ex:
+        futs = [ex.submit(_run, j, verbose) for j in jobs]
+        if synth_cmd:
+            futs.append(ex.submit(_run, synth_cmd, verbose))
+        for f in futs:
+            f.result()
+    if _stale(LIB, objs):
+        _run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs, verbose)
+    return {"libmocatt": LIB, "libmocsynth": SYNTH_LIB}
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,211 @@
+// moc_device.cuh — device helpers shared by the sweep kernels (sm_103a).
+//
+// Vector loads of table rows, vector tally reductions (red.global.add.v4.f32, sm_90+),
+// the exponential in its two evaluation modes, and the reciprocal.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace moc {
+
+// ------------------------------------------------------------------------------------
+// Row vectors: VEC consecutive groups held by one lane.
+// ------------------------------------------------------------------------------------
+template <int VEC>
+struct Vec {
+    float v[VEC];
+};
+
+// Read-only row load through the non-coherent path, kept in L2 (rows are re-read by
+// many segments). Requires 4*VEC-byte alignment.
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> ld_row(const float *p)
+{
+    Vec<VEC> r;
+    if constexpr (VEC == 4) {
+        float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+        r.v[0] = x.x; r.v[1] = x.y; r.v[2] = x.z; r.v[3] = x.w;
+    } else if constexpr (VEC == 2) {
+        float2 x = __ldg(reinterpret_cast<const float2 *>(p));
+        r.v[0] = x.x; r.v[1] = x.y;
+    } else {
+        r.v[0] = __ldg(p);
+    }
+    return r;
+}
+
+// Plain (coherent) row load/store for psi, which the sweep owns.
+template <int VEC>
+__device__ __forceinline__ Vec<VEC> ld_psi(const float *p, int n_valid)
+{
+    Vec<VEC> r;
+    if (n_valid >= VEC) {
+        if constexpr (VEC == 4) {
+            float4 x = *reinterpret_cast<const float4 *>(p);
+            r.v[0] = x.x; r.v[1] = x.y; r.v[2] = x.z; r.v[3] = x.w;
+        } else if constexpr (VEC == 2) {
+            float2 x = *reinterpret_cast<const float2 *>(p);
+            r.v[0] = x.x; r.v[1] = x.y;
+        } else {
+            r.v[0] = *p;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VEC; k++) r.v[k] = k < n_valid ? p[k] : 0.0f;
+    }
+    return r;
+}
+
+template <int VEC>
+__device__ __forceinline__ void st_psi(float *p, const Vec<VEC> &r, int n_valid)
+{
+    if (n_valid >= VEC) {
+        if constexpr (VEC == 4) {
+            *reinterpret_cast<float4 *>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+        } else if constexpr (VEC == 2) {
+            *reinterpret_cast<float2 *>(p) = make_float2(r.v[0], r.v[1]);
+        } else {
+            *p = r.v[0];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VEC; k++)
+            if (k < n_valid) p[k] = r.v[k];
+    }
+}
+
+// Streaming load of a per-segment descriptor field (read once; evict first).
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p)
+{
+    return __ldcs(p);
+}
+
+// ------------------------------------------------------------------------------------
+// Tally reduction: fine_flux[cell][g0 .. g0+VEC) += t. Vector reductions are one L2
+// atomic request per lane instead of VEC. Lanes whose row is only partly inside the
+// group range fall back to scalar reductions so padding entries are never written.
+// ------------------------------------------------------------------------------------
+template <int VEC>
+__device__ __forceinline__ void red_row(float *p, const Vec<VEC> &t, int n_valid)
+{
+    if (n_valid >= VEC) {
+        if constexpr (VEC == 4) {
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p),
+                         "f"(t.v[0]), "f"(t.v[1]), "f"(t.v[2]), "f"(t.v[3])
+                         : "memory");
+        } else if constexpr (VEC == 2) {
+            asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(t.v[0]),
+                         "f"(t.v[1])
+                         : "memory");
+        } else {
+            asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(t.v[0]) : "memory");
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < VEC; k++)
+            if (k < n_valid)
+                asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p + k), "f"(t.v[k])
+                             : "memory");
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Arithmetic helpers.
+// ------------------------------------------------------------------------------------
+
+// Hardware reciprocal approximation (MUFU.RCP), about 1 ulp.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Hardware base-2 exponential (MUFU.EX2), about 2 ulp; the unit splits its argument into
+// integer and fraction itself.
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// exp(-tau) for tau >= 0 with a Cody-Waite split of the argument (Cody & Waite, 1980):
+// x = -tau * log2(e) is formed as hi + lo, where hi is the rounded product and lo the
+// rounding error of that product plus the tail of log2(e); 2^x = 2^hi * (1 + lo ln 2).
+// The split removes the error of rounding x, which grows with |x|; what is left is the
+// error of ex2.approx itself.
+__device__ __forceinline__ float exp_neg_rr(float tau)
+{
+    const float L2E_HI = 1.44269502162933349609375f;     // float nearest log2(e)
+    const float L2E_LO = 1.9259629911266175e-8f;         // log2(e) - L2E_HI
+    const float LN2 = 0.693147180559945309f;
+    const float hi = -tau * L2E_HI;
+    const float lo = fmaf(-tau, L2E_HI, -hi) - tau * L2E_LO;
+    const float p = ex2_approx(hi);
+    return fmaf(p, lo * LN2, p);
+}
+
+// -expm1(-tau) = 1 - exp(-tau) for 0 <= tau < 0.25 by its Taylor series
+// tau - tau^2/2! + tau^3/3! - ... (8 terms; truncation below 2^-24 relative).
+__device__ __forceinline__ float one_minus_exp_series(float tau)
+{
+    float s = 1.0f / 40320.0f;                  // 1/8!
+    s = fmaf(s, -tau, 1.0f / 5040.0f);          // 1/7!
+    s = fmaf(s, -tau, 1.0f / 720.0f);
+    s = fmaf(s, -tau, 1.0f / 120.0f);
+    s = fmaf(s, -tau, 1.0f / 24.0f);
+    s = fmaf(s, -tau, 1.0f / 6.0f);
+    s = fmaf(s, -tau, 0.5f);
+    s = fmaf(s, -tau, 1.0f);
+    return s * tau;
+}
+
+// tau - (1 - exp(-tau)) = tau^2/2! - tau^3/3! + ... for 0 <= tau < 0.25.
+__device__ __forceinline__ float tau_minus_e_series(float tau)
+{
+    float s = 1.0f / 40320.0f;                  // 1/8!
+    s = fmaf(s, -tau, 1.0f / 5040.0f);
+    s = fmaf(s, -tau, 1.0f / 720.0f);
+    s = fmaf(s, -tau, 1.0f / 120.0f);
+    s = fmaf(s, -tau, 1.0f / 24.0f);
+    s = fmaf(s, -tau, 1.0f / 6.0f);
+    s = fmaf(s, -tau, 0.5f);
+    return s * tau * tau;
+}
+
+// tau(tau(tau-3)+6) - 6(1 - exp(-tau)) = 6 (tau^4/4! - tau^5/5! + ...) for
+// 0 <= tau < 0.5 (terms through tau^12).
+__device__ __forceinline__ float cubic_series(float tau)
+{
+    float s = 1.0f / 479001600.0f;              // 1/12!
+    s = fmaf(s, -tau, 1.0f / 39916800.0f);      // 1/11!
+    s = fmaf(s, -tau, 1.0f / 3628800.0f);
+    s = fmaf(s, -tau, 1.0f / 362880.0f);
+    s = fmaf(s, -tau, 1.0f / 40320.0f);
+    s = fmaf(s, -tau, 1.0f / 5040.0f);
+    s = fmaf(s, -tau, 1.0f / 720.0f);
+    s = fmaf(s, -tau, 1.0f / 120.0f);
+    s = fmaf(s, -tau, 1.0f / 24.0f);
+    const float t2 = tau * tau;
+    return 6.0f * s * t2 * t2;
+}
+
+// The reference's table lookup (src/cpu/kernel.c:337-361), rounded exactly as the
+// reference's C rounds it: IEEE division, no contraction, truncating conversion.
+// tab holds (slope, intercept) pairs in shared memory.
+__device__ __forceinline__ float table_lookup(const float2 *tab, int n_points, float dx,
+                                              float lookup_max, float x)
+{
+    if (x > lookup_max) return 1.0f;
+    const float q = __fdiv_rn(x, dx);
+    const float h = __fmul_rn(0.5f, dx);
+    int n = __float2int_rz(__fadd_rn(q, h));
+    n = n < 0 ? 0 : (n >= n_points ? n_points - 1 : n);  // never taken for x in domain
+    const float2 si = tab[n];
+    return __fadd_rn(__fmul_rn(si.x, x), si.y);
+}
+
+}  // namespace moc

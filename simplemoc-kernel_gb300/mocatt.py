@@ -1,0 +1,399 @@
+"""Python binding of the GB300 segment-attenuation library (ctypes over the C ABI).
+
+This is glue for tests and the bench: the product is libmocatt.so and its C ABI
+(include/moc_attenuate.h). Every compute call goes through that ABI; there is no Python
+or CPU compute path here, and loading fails loudly if the library was not built.
+
+Workloads are named by what they are: the reference's CPU-sized sweep
+(`sweep_1M_g64`, the reference's `-s 1000000 -e 64`), the 50M x 128 sweep
+(`sweep_50M_g128`, the reference's default problem size), the wide-tau precision
+workload, the lognormal-track batch, and the adjoint workload.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+BUILD = os.path.join(PKG, "_build")
+
+# ------------------------------------------------------------------------------------
+# C structs (must match include/moc_attenuate.h and include/moc_synth.h)
+# ------------------------------------------------------------------------------------
+MOC_OK = 0
+MOC_ERR_INVALID_ARG = 1
+MOC_ERR_MISALIGNED = 2
+MOC_ERR_UNSUPPORTED = 3
+MOC_ERR_CUDA = 4
+MOC_ERR_NO_DEVICE = 5
+MOC_ERR_OUT_OF_MEMORY = 6
+MOC_ERR_BAD_INDEX = 7
+MOC_ERR_DEVICE_TIMEOUT = 8
+
+MOC_EXP_FULL = 0
+MOC_EXP_TABLE = 1
+MOC_PREC_FP32 = 0
+MOC_PREC_BF16 = 1
+MOC_PREC_FP16 = 2
+MOC_TALLY_ATOMIC_FP32 = 0
+MOC_TALLY_COMPENSATED = 1
+MOC_TALLY_FP64 = 2
+
+
+class MocProblem(C.Structure):
+    _fields_ = [
+        ("n_regions", C.c_int32), ("n_intervals", C.c_int32), ("n_groups", C.c_int32),
+        ("group_stride", C.c_int32), ("n_tracks", C.c_int32), ("reserved0", C.c_int32),
+        ("n_segments", C.c_int64),
+        ("track_offsets", C.c_void_p), ("seg_region", C.c_void_p),
+        ("seg_interval", C.c_void_p), ("seg_ds", C.c_void_p),
+        ("sigT", C.c_void_p), ("source", C.c_void_p), ("fine_flux", C.c_void_p),
+        ("psi", C.c_void_p),
+    ]
+
+
+class MocFwdOpts(C.Structure):
+    _fields_ = [
+        ("exp_mode", C.c_int), ("table_points", C.c_int32), ("table_max", C.c_float),
+        ("precision", C.c_int), ("tally", C.c_int),
+        ("dz", C.c_float), ("zin", C.c_float), ("weight", C.c_float), ("mu", C.c_float),
+        ("mu2", C.c_float), ("checked", C.c_int32), ("vec", C.c_int32),
+        ("warps_per_block", C.c_int32), ("reserved", C.c_int32 * 4),
+    ]
+
+
+class SynthSpec(C.Structure):
+    _fields_ = [
+        ("seed", C.c_uint64), ("n_regions", C.c_int32), ("n_intervals", C.c_int32),
+        ("n_groups", C.c_int32), ("group_stride", C.c_int32), ("n_tracks", C.c_int32),
+        ("n_segments", C.c_int64), ("track_mode", C.c_int32), ("len_median", C.c_float),
+        ("len_sigma", C.c_float), ("len_min", C.c_int32), ("len_max", C.c_int32),
+        ("sigT_mode", C.c_int32), ("sigT_lo", C.c_float), ("sigT_hi", C.c_float),
+        ("ds_lo", C.c_float), ("ds_hi", C.c_float),
+    ]
+
+
+# Symbols the C ABI exports (include/moc_attenuate.h), with ctypes signatures.
+_P = C.c_void_p
+ABI = {
+    "moc_fwd_opts_default": (None, [C.POINTER(MocFwdOpts)]),
+    "moc_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "moc_destroy": (C.c_int, [_P]),
+    "moc_attenuate_fwd": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts), _P]),
+    "moc_attenuate_fwd_host": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts)]),
+    "moc_synchronize": (C.c_int, [_P, _P]),
+    "moc_build_exp_table": (C.c_int, [C.c_int32, C.c_float, _P, C.POINTER(C.c_float),
+                                      C.POINTER(C.c_float)]),
+    "moc_status_string": (C.c_char_p, [C.c_int]),
+    "moc_last_error": (C.c_char_p, [_P]),
+    "moc_abi_version": (C.c_int32, []),
+}
+SYNTH_ABI = {
+    "moc_synth_spec_init": (None, [C.POINTER(SynthSpec), C.c_uint64, C.c_int32, C.c_int32,
+                                   C.c_int32, C.c_int32, C.c_int64]),
+    "moc_synth_track_offsets": (C.c_int64, [C.POINTER(SynthSpec), _P]),
+    "moc_synth_fill": (C.c_int, [C.POINTER(SynthSpec), _P, _P, _P, _P, _P, _P, _P]),
+    "moc_synth_uniform": (None, [C.c_uint64, C.c_uint64, C.c_int64, C.c_float, C.c_float, _P]),
+    "moc_synth_normal": (None, [C.c_uint64, C.c_uint64, C.c_int64, _P]),
+    "moc_synth_randint": (None, [C.c_uint64, C.c_uint64, C.c_int64, C.c_int64, _P]),
+}
+
+_lib = None
+_synth = None
+
+
+def _bind(path: str, table: dict):
+    if not os.path.exists(path):
+        raise RuntimeError(f"{os.path.basename(path)} is not built ({path}); run "
+                           "__graft_entry__.build() first")
+    lib = C.CDLL(path)
+    for name, (res, args) in table.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def lib():
+    """The loaded libmocatt.so (raises if it is missing)."""
+    global _lib
+    if _lib is None:
+        _lib = _bind(os.path.join(BUILD, "libmocatt.so"), ABI)
+    return _lib
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        _synth = _bind(os.path.join(BUILD, "libmocsynth.so"), SYNTH_ABI)
+    return _synth
+
+
+class MocError(RuntimeError):
+    def __init__(self, status: int, detail: str = ""):
+        self.status = status
+        msg = lib().moc_status_string(status).decode()
+        super().__init__(f"moc status {status} ({msg}){': ' + detail if detail else ''}")
+
+
+def default_opts(**kw) -> MocFwdOpts:
+    o = MocFwdOpts()
+    lib().moc_fwd_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def build_exp_table(n_points: int, max_val: float):
+    vals = np.zeros(2 * n_points, np.float32)
+    dx, lk = C.c_float(), C.c_float()
+    st = lib().moc_build_exp_table(n_points, max_val, vals.ctypes.data, C.byref(dx), C.byref(lk))
+    if st:
+        raise MocError(st)
+    return vals, dx.value, lk.value
+
+
+# ------------------------------------------------------------------------------------
+# Workloads
+# ------------------------------------------------------------------------------------
+@dataclasses.dataclass(frozen=True)
+class Workload:
+    name: str
+    seed: int
+    regions: int
+    intervals: int
+    groups: int
+    tracks: int
+    segments: int = 0            # uniform track assignment (0 with lognormal lengths)
+    lognormal: tuple | None = None   # (median, sigma, min, max)
+    logsigt: tuple | None = None     # sigT ~ logU(lo, hi)
+    ds: tuple = (0.01, 1.0)
+
+    def with_(self, **kw) -> "Workload":
+        return dataclasses.replace(self, **kw)
+
+    def spec(self) -> SynthSpec:
+        s = SynthSpec()
+        synth_lib().moc_synth_spec_init(C.byref(s), self.seed, self.regions, self.intervals,
+                                        self.groups, self.tracks, self.segments)
+        if self.lognormal:
+            s.track_mode = 1
+            s.len_median, s.len_sigma, s.len_min, s.len_max = self.lognormal
+        if self.logsigt:
+            s.sigT_mode = 1
+            s.sigT_lo, s.sigT_hi = self.logsigt
+        s.ds_lo, s.ds_hi = self.ds
+        return s
+
+    def cpu_bench_args(self) -> list[str]:
+        a = ["--seed", str(self.seed), "--regions", str(self.regions), "--intervals",
+             str(self.intervals), "--groups", str(self.groups), "--tracks", str(self.tracks),
+             "--segments", str(self.segments), "--ds", str(self.ds[0]), str(self.ds[1])]
+        if self.lognormal:
+            a += ["--lognormal"] + [str(x) for x in self.lognormal]
+        if self.logsigt:
+            a += ["--logsigt"] + [str(x) for x in self.logsigt]
+        return a
+
+
+# lognormal track lengths: median 200, sigma = sqrt(2 ln 1.5) so the mean is 300
+LOGN_BATCH = (200.0, 0.9005, 1, 5000)
+# 5,000 tracks, about 2,000,000 segments: same sigma, median 400 / exp(sigma^2 / 2)
+LOGN_ADJ = (267.0, 0.9005, 1, 5000)
+
+WORKLOADS = {
+    # the reference's CPU-sized run (-s 1000000 -e 64), 1,000 tracks, 2,000 regions
+    "sweep_1M_g64": Workload("sweep_1M_g64", 1, 2000, 5, 64, 1000, 1_000_000),
+    # the reference's default size (-s 50000000 -e 128), 100,000 tracks, 10,000 regions
+    "sweep_50M_g128": Workload("sweep_50M_g128", 2, 10000, 5, 128, 100_000, 50_000_000),
+    # same shapes, tau spread over ~[1e-6, 40] for the precision form
+    "widetau_50M_g128": Workload("widetau_50M_g128", 2, 10000, 5, 128, 100_000, 50_000_000,
+                                 logsigt=(1e-3, 20.0), ds=(1e-3, 2.0)),
+    # three problems of 20,000 lognormal tracks (about 6M segments each)
+    "batch_20k_g16": Workload("batch_20k_g16", 3, 2000, 5, 16, 20_000, 0, LOGN_BATCH),
+    "batch_20k_g70": Workload("batch_20k_g70", 3, 2000, 5, 70, 20_000, 0, LOGN_BATCH),
+    "batch_20k_g128": Workload("batch_20k_g128", 3, 2000, 5, 128, 20_000, 0, LOGN_BATCH),
+    # adjoint: 5,000 lognormal tracks, about 2M segments, G=64
+    "adjoint_2M_g64": Workload("adjoint_2M_g64", 4, 2000, 5, 64, 5000, 0, LOGN_ADJ),
+}
+
+
+@dataclasses.dataclass
+class HostProblem:
+    """A problem's arrays in host memory (numpy), in the C ABI's layout."""
+    R: int
+    I: int
+    G: int
+    Gs: int
+    T: int
+    S: int
+    track_offsets: np.ndarray   # int64 [T+1]
+    seg_region: np.ndarray      # int32 [S]
+    seg_interval: np.ndarray    # uint8 [S]
+    seg_ds: np.ndarray          # float32 [S]
+    sigT: np.ndarray            # float32 [R, Gs]
+    source: np.ndarray          # float32 [R*I, Gs]
+    fine_flux: np.ndarray       # float32 [R*I, Gs]
+    psi: np.ndarray             # float32 [T, Gs]
+
+    def copy(self) -> "HostProblem":
+        return dataclasses.replace(self, **{f.name: getattr(self, f.name).copy()
+                                            for f in dataclasses.fields(self)
+                                            if isinstance(getattr(self, f.name), np.ndarray)})
+
+    def c_struct(self) -> MocProblem:
+        """C struct pointing at these (host) arrays; keep self alive while it is used."""
+        for name in ("track_offsets", "seg_region", "seg_interval", "seg_ds", "sigT",
+                     "source", "fine_flux", "psi"):
+            a = getattr(self, name)
+            assert a.flags["C_CONTIGUOUS"], name
+        return MocProblem(self.R, self.I, self.G, self.Gs, self.T, 0, self.S,
+                          self.track_offsets.ctypes.data, self.seg_region.ctypes.data,
+                          self.seg_interval.ctypes.data, self.seg_ds.ctypes.data,
+                          self.sigT.ctypes.data, self.source.ctypes.data,
+                          self.fine_flux.ctypes.data, self.psi.ctypes.data)
+
+    def subset_tracks(self, tracks) -> "HostProblem":
+        """A problem with only the given tracks (same tables, fresh zero tallies). psi of a
+        track depends only on its own segments, so this reproduces those tracks exactly."""
+        tracks = np.asarray(tracks, np.int64)
+        lens = self.track_offsets[tracks + 1] - self.track_offsets[tracks]
+        off = np.zeros(len(tracks) + 1, np.int64)
+        off[1:] = np.cumsum(lens)
+        idx = np.concatenate([np.arange(self.track_offsets[t], self.track_offsets[t + 1])
+                              for t in tracks]) if len(tracks) else np.zeros(0, np.int64)
+        return HostProblem(self.R, self.I, self.G, self.Gs, len(tracks), int(off[-1]), off,
+                           self.seg_region[idx].copy(), self.seg_interval[idx].copy(),
+                           self.seg_ds[idx].copy(), self.sigT, self.source,
+                           np.zeros_like(self.fine_flux), self.psi[tracks].copy())
+
+
+def _aligned_empty(shape, dtype, align=64):
+    """numpy array with 64-byte aligned data (the ABI wants 16-byte aligned rows)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    buf = np.empty(n + align, np.uint8)
+    off = (-buf.ctypes.data) % align
+    return buf[off:off + n].view(dtype).reshape(shape)
+
+
+def generate(w: Workload, group_stride: int | None = None) -> HostProblem:
+    """Seeded inputs of a workload (moc_synth.h), fine_flux zeroed."""
+    sl = synth_lib()
+    spec = w.spec()
+    if group_stride is not None:
+        spec.group_stride = group_stride
+    T, Gs, R, I = w.tracks, spec.group_stride, w.regions, w.intervals
+    off = np.zeros(T + 1, np.int64)
+    S = sl.moc_synth_track_offsets(C.byref(spec), off.ctypes.data)
+    if S < 0:
+        raise ValueError(f"invalid workload {w}")
+    psi = _aligned_empty((T, Gs), np.float32)
+    sig = _aligned_empty((R, Gs), np.float32)
+    src = _aligned_empty((R * I, Gs), np.float32)
+    reg = np.empty(S, np.int32)
+    itv = np.empty(S, np.uint8)
+    ds = np.empty(S, np.float32)
+    if sl.moc_synth_fill(C.byref(spec), off.ctypes.data, psi.ctypes.data, sig.ctypes.data,
+                         src.ctypes.data, reg.ctypes.data, itv.ctypes.data, ds.ctypes.data):
+        raise ValueError("moc_synth_fill failed")
+    ff = _aligned_empty((R * I, Gs), np.float32)
+    ff[:] = 0
+    return HostProblem(R, I, w.groups, Gs, T, int(S), off, reg, itv, ds, sig, src, ff, psi)
+
+
+def synth_normal(seed: int, tag: int, n: int) -> np.ndarray:
+    out = np.empty(n, np.float32)
+    synth_lib().moc_synth_normal(seed, tag, n, out.ctypes.data)
+    return out
+
+
+def synth_uniform(seed: int, tag: int, n: int, lo: float, hi: float) -> np.ndarray:
+    out = np.empty(n, np.float32)
+    synth_lib().moc_synth_uniform(seed, tag, n, lo, hi, out.ctypes.data)
+    return out
+
+
+def synth_randint(seed: int, tag: int, n: int, bound: int) -> np.ndarray:
+    out = np.empty(n, np.int64)
+    synth_lib().moc_synth_randint(seed, tag, n, bound, out.ctypes.data)
+    return out
+
+
+# ------------------------------------------------------------------------------------
+# Device side (torch is only the allocator and stream provider here)
+# ------------------------------------------------------------------------------------
+class DeviceProblem:
+    """A problem resident on the GPU (torch tensors), and its C struct."""
+
+    NAMES = ("track_offsets", "seg_region", "seg_interval", "seg_ds", "sigT", "source",
+             "fine_flux", "psi")
+
+    def __init__(self, hp: HostProblem, device="cuda:0"):
+        import torch
+        self.R, self.I, self.G, self.Gs, self.T, self.S = hp.R, hp.I, hp.G, hp.Gs, hp.T, hp.S
+        for n in self.NAMES:
+            a = getattr(hp, n)
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(device) if a.size else \
+                torch.empty(max(1, a.size), dtype=torch.from_numpy(a).dtype, device=device)
+            setattr(self, n, t)
+
+    def c_struct(self) -> MocProblem:
+        return MocProblem(self.R, self.I, self.G, self.Gs, self.T, 0, self.S,
+                          *[getattr(self, n).data_ptr() for n in self.NAMES])
+
+    def to_host(self, name):
+        return getattr(self, name).cpu().numpy()
+
+
+class Handle:
+    """Owns a moc_handle_t."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        st = lib().moc_create(C.byref(self._h), device)
+        if st:
+            raise MocError(st)
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def check(self, st: int):
+        if st:
+            raise MocError(st, lib().moc_last_error(self._h).decode())
+
+    def fwd(self, dp: DeviceProblem, opts: MocFwdOpts | None = None, stream=None):
+        """moc_attenuate_fwd on the device problem, on `stream` (a torch stream or None
+        for torch's current stream)."""
+        import torch
+        opts = opts or default_opts()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        prob = dp.c_struct()
+        self.check(lib().moc_attenuate_fwd(self._h, C.byref(prob), C.byref(opts),
+                                           C.c_void_p(s.cuda_stream)))
+
+    def fwd_host(self, hp: HostProblem, opts: MocFwdOpts | None = None):
+        opts = opts or default_opts()
+        prob = hp.c_struct()
+        self.check(lib().moc_attenuate_fwd_host(self._h, C.byref(prob), C.byref(opts)))
+
+    def synchronize(self, stream=None) -> int:
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return lib().moc_synchronize(self._h, C.c_void_p(s.cuda_stream))
+
+    def close(self):
+        if self._h:
+            lib().moc_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
