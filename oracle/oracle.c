@@ -279,10 +279,16 @@ static expo_t expo_exact(double tau)
     x.E = exp(-tau);
     x.e = -expm1(-tau);
     if (tau < 1.0) {
+        static const double inv[40] = {
+            0, 1, 1. / 2, 1. / 3, 1. / 4, 1. / 5, 1. / 6, 1. / 7, 1. / 8, 1. / 9, 1. / 10,
+            1. / 11, 1. / 12, 1. / 13, 1. / 14, 1. / 15, 1. / 16, 1. / 17, 1. / 18, 1. / 19,
+            1. / 20, 1. / 21, 1. / 22, 1. / 23, 1. / 24, 1. / 25, 1. / 26, 1. / 27, 1. / 28,
+            1. / 29, 1. / 30, 1. / 31, 1. / 32, 1. / 33, 1. / 34, 1. / 35, 1. / 36, 1. / 37,
+            1. / 38, 1. / 39};
         double term = tau, s2 = 0.0, s3 = 0.0, s4 = 0.0;
         const double stop = 1e-18 * tau * tau * tau * tau / 24.0;
         for (int k = 2; k < 40; k++) {
-            term *= tau / k;
+            term *= tau * inv[k];
             const double st = (k & 1) ? -term : term;
             s2 += st;
             if (k >= 3) s3 += st;
@@ -321,25 +327,29 @@ typedef struct {
     const double *source; /* [R][I][Gs] */
     table_t tab;
     double dz, zin, weight, mu, mu2;
+    double *q;            /* [R*I][3][Gs] fitted q0, q1, q2           */
+    double *aq;           /* [R*I][3][Gs] their error magnitudes       */
 } ctx64_t;
 
 /* q0,q1,q2 of cell (r, i) for group g, and their error magnitudes. */
-static void q_of(const ctx64_t *c, int32_t r, int32_t i, int g, double q[3], double aq[3])
+static inline void q_of(const ctx64_t *c, int32_t r, int32_t i, int g, double q[3],
+                        double aq[3])
 {
-    const int I = c->p->n_intervals;
     const int64_t Gs = c->p->group_stride;
-    double a[3][3];
-    qfit_coeffs(i, I, c->dz, c->zin, a);
+    const int64_t b = ((int64_t)r * c->p->n_intervals + i) * 3 * Gs + g;
     for (int k = 0; k < 3; k++) {
-        q[k] = 0.0;
-        aq[k] = 0.0;
-        for (int m = -1; m <= 1; m++) {
-            if (a[k][m + 1] == 0.0) continue;
-            const double y = c->source[((int64_t)r * I + i + m) * Gs + g];
-            q[k] += a[k][m + 1] * y;
-            aq[k] += fabs(a[k][m + 1] * y);
-        }
+        q[k] = c->q[b + k * Gs];
+        aq[k] = c->aq[b + k * Gs];
     }
+}
+
+static void ctx_free(ctx64_t *c)
+{
+    free(c->tab.values);
+    free(c->q);
+    free(c->aq);
+    c->tab.values = NULL;
+    c->q = c->aq = NULL;
 }
 
 static int ctx_init(ctx64_t *c, const moc_problem_t *p, const moc_fwd_opts_t *o,
@@ -354,7 +364,33 @@ static int ctx_init(ctx64_t *c, const moc_problem_t *p, const moc_fwd_opts_t *o,
     c->weight = o->weight;
     c->mu = o->mu;
     c->mu2 = o->mu2;
-    return table_make(o, &c->tab);
+    const int64_t I = p->n_intervals, Gs = p->group_stride, G = p->n_groups;
+    const int64_t ncell = (int64_t)p->n_regions * I;
+    c->q = (double *)calloc((size_t)(ncell * 3 * Gs), sizeof(double));
+    c->aq = (double *)calloc((size_t)(ncell * 3 * Gs), sizeof(double));
+    c->tab.values = NULL;
+    if (!c->q || !c->aq || table_make(o, &c->tab)) {
+        ctx_free(c);
+        return -1;
+    }
+    for (int64_t cell = 0; cell < ncell; cell++) {
+        const int i = (int)(cell % I);
+        double a[3][3];
+        qfit_coeffs(i, (int)I, c->dz, c->zin, a);
+        for (int k = 0; k < 3; k++)
+            for (int64_t g = 0; g < G; g++) {
+                double q = 0.0, aq = 0.0;
+                for (int m = -1; m <= 1; m++) {
+                    if (a[k][m + 1] == 0.0) continue;
+                    const double y = source[(cell + m) * Gs + g];
+                    q += a[k][m + 1] * y;
+                    aq += fabs(a[k][m + 1] * y);
+                }
+                c->q[(cell * 3 + k) * Gs + g] = q;
+                c->aq[(cell * 3 + k) * Gs + g] = aq;
+            }
+    }
+    return 0;
 }
 
 static double *promote(const float *x, int64_t n)
@@ -431,10 +467,10 @@ int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi
                                       q[2] * c.mu2 * reuse + psi[g] * x.E;
                     /* error magnitudes (see oracle.h); em bounds |e| plus its absolute
                      * evaluation error (1 - expf(-tau) is off by ~2^-24 absolutely) */
-                    const double em = 1.0 + x.e;
+                    const double em = 1.0 + fabs(x.e);
                     const double areuse = tau * (tau + 2.0) + 2.0 * em / s3;
                     const double afi = (aq[0] * tau + (s * fabs(psi[g]) + aq[0]) * em) / s2 +
-                                       apsi[g] * x.e / s + aq[1] * c.mu * areuse +
+                                       apsi[g] * fabs(x.e) / s + aq[1] * c.mu * areuse +
                                        aq[2] * c.mu2 *
                                            (tau * tau * tau + 3.0 * tau * tau + 6.0 * tau +
                                             6.0 * em) / (3.0 * s4);
@@ -477,7 +513,7 @@ int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi
     if (abs_tally) memcpy(abs_tally, atal, (size_t)nff * sizeof(double));
     if (hits) memcpy(hits, nh, (size_t)ncell * sizeof(int64_t));
     free(sig); free(src); free(ff); free(aff); free(atal); free(nh);
-    free(c.tab.values);
+    ctx_free(&c);
     return 0;
 }
 
@@ -642,7 +678,7 @@ int oracle_adj_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, const doubl
             }
         }
     free(sig); free(src); free(dq); free(dsc);
-    free(c.tab.values);
+    ctx_free(&c);
     return 0;
 }
 
@@ -682,6 +718,6 @@ double oracle_loss_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o,
             L += v[(int64_t)t * Gs + g] * psi;
         }
     }
-    free(c.tab.values);
+    ctx_free(&c);
     return L;
 }

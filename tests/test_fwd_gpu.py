@@ -1,0 +1,179 @@
+"""Parity of the GPU forward sweep (through the C ABI) with the CPU oracle."""
+import numpy as np
+import pytest
+
+import mocatt
+import oracle
+import parity
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(handle, hp, opts=None, device="cuda:0"):
+    dp = mocatt.DeviceProblem(hp, device)
+    handle.fwd(dp, opts)
+    st = handle.synchronize()
+    assert st == 0, mocatt.lib().moc_status_string(st)
+    return dp.to_host("psi"), dp.to_host("fine_flux")
+
+
+def small(name="sweep_1M_g64", **kw):
+    base = dict(regions=120, tracks=48, segments=12_000)
+    base.update(kw)
+    return mocatt.generate(mocatt.WORKLOADS[name].with_(**base))
+
+
+def test_plain_sweep_1M_g64_full_size(handle):
+    """The reference's CPU-sized run (1,000,000 segments, G=64) at full size."""
+    hp = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"])
+    psi, ff = run_gpu(handle, hp)
+    ref = oracle.fwd_fp64(hp)
+    res = parity.check_plain(psi, ff, ref, hp.G)
+    # and against the FP32 restatement of the reference itself
+    p32, f32 = oracle.fwd_fp32(hp)
+    parity.check_plain(p32, f32, ref, hp.G)
+    print(res, parity.rel_err(psi[:, :hp.G], p32[:, :hp.G]))
+
+
+@pytest.mark.parametrize("G", [1, 3, 16, 32, 64, 70, 128, 130, 256])
+def test_plain_group_counts(handle, G):
+    hp = small(groups=G)
+    psi, ff = run_gpu(handle, hp)
+    parity.check_plain(psi, ff, oracle.fwd_fp64(hp), G)
+    # padding entries are never written
+    if hp.Gs > G:
+        assert np.all(ff[:, G:] == 0)
+
+
+@pytest.mark.parametrize("vec", [1, 2, 4])
+@pytest.mark.parametrize("wpb", [1, 4, 8])
+def test_plain_launch_shapes(handle, vec, wpb):
+    hp = small(groups=64)
+    psi, ff = run_gpu(handle, hp, mocatt.default_opts(vec=vec, warps_per_block=wpb))
+    parity.check_plain(psi, ff, oracle.fwd_fp64(hp), hp.G)
+
+
+@pytest.mark.parametrize("npts,maxv", [(353, 10.0), (10_000, 10.0), (50, 3.0)])
+def test_table_mode_matches_reference_table(handle, npts, maxv):
+    """Table mode: e is the reference's lookup, bit for bit; the rest within tolerance."""
+    hp = small(groups=64)
+    opts = mocatt.default_opts(exp_mode=mocatt.MOC_EXP_TABLE, table_points=npts,
+                               table_max=maxv)
+    psi, ff = run_gpu(handle, hp, opts)
+    ref = oracle.fwd_fp64(hp, opts)
+    parity.check_plain(psi, ff, ref, hp.G)
+
+
+def test_psi_deterministic_and_tally_additive(handle):
+    hp = small(groups=64)
+    p1, f1 = run_gpu(handle, hp)
+    p2, f2 = run_gpu(handle, hp)
+    assert np.array_equal(p1, p2)           # psi has no reduction: bitwise
+    # tallies arrive in another order each run: both inside the FP32 tolerance
+    ref = oracle.fwd_fp64(hp)
+    parity.check_plain(p1, f1, ref, hp.G)
+    parity.check_plain(p2, f2, ref, hp.G)
+    # tallies add into what fine_flux held
+    hp2 = hp.copy()
+    hp2.fine_flux[:] = f1
+    p3, f3 = run_gpu(handle, hp2)
+    parity.check_plain(p3, f3, oracle.fwd_fp64(hp2), hp.G)
+
+
+def test_empty_and_ragged_tracks(handle):
+    hp = small(groups=64, tracks=300, segments=400)  # many empty / 1-segment tracks
+    lens = np.diff(hp.track_offsets)
+    assert (lens == 0).any() and (lens == 1).any()
+    psi, ff = run_gpu(handle, hp)
+    parity.check_plain(psi, ff, oracle.fwd_fp64(hp), hp.G)
+    empty = lens == 0
+    np.testing.assert_array_equal(psi[empty], hp.psi[empty])
+
+
+def test_zero_tracks_and_zero_segments(handle):
+    hp = small(groups=16, tracks=5, segments=0)
+    psi, ff = run_gpu(handle, hp)
+    np.testing.assert_array_equal(psi, hp.psi)
+    assert not ff.any()
+
+
+def test_host_entry_point_matches_device(handle):
+    hp = small(groups=64)
+    psi_d, ff_d = run_gpu(handle, hp)
+    q = hp.copy()
+    handle.fwd_host(q)
+    assert np.array_equal(q.psi, psi_d)
+    np.testing.assert_allclose(q.fine_flux, ff_d, rtol=1e-5, atol=1e-6)
+
+
+def test_bad_index_is_skipped_and_reported(handle):
+    """A segment with an out-of-range region is skipped by the kernel's own bounds check
+    and reported; checked mode rejects the problem before touching anything."""
+    hp = small(groups=16)
+    hp.seg_region[5] = hp.R + 7
+    dp = mocatt.DeviceProblem(hp)
+    opts = mocatt.default_opts(checked=1)
+    st = mocatt.lib().moc_attenuate_fwd(handle.ptr, mocatt.C.byref(dp.c_struct()),
+                                        mocatt.C.byref(opts), None)
+    assert st == mocatt.MOC_ERR_BAD_INDEX
+    np.testing.assert_array_equal(dp.to_host("psi"), hp.psi)
+    assert not dp.to_host("fine_flux").any()
+    handle.fwd(dp)
+    assert handle.synchronize() == mocatt.MOC_ERR_BAD_INDEX
+    assert handle.synchronize() == 0  # cleared
+
+
+def test_invalid_arguments_return_status(handle):
+    hp = small(groups=16)
+    dp = mocatt.DeviceProblem(hp)
+    L = mocatt.lib()
+    o = mocatt.default_opts()
+
+    def call(prob, opts=o):
+        return L.moc_attenuate_fwd(handle.ptr, mocatt.C.byref(prob), mocatt.C.byref(opts), None)
+
+    p = dp.c_struct(); p.group_stride = 18
+    assert call(p) == mocatt.MOC_ERR_UNSUPPORTED
+    p = dp.c_struct(); p.n_intervals = 1
+    assert call(p) == mocatt.MOC_ERR_INVALID_ARG
+    p = dp.c_struct(); p.sigT = dp.sigT.data_ptr() + 4
+    assert call(p) == mocatt.MOC_ERR_MISALIGNED
+    p = dp.c_struct(); p.psi = None
+    assert call(p) == mocatt.MOC_ERR_INVALID_ARG
+    p = dp.c_struct(); p.sigT = hp.sigT.ctypes.data   # host pointer to the device entry
+    assert call(p) == mocatt.MOC_ERR_INVALID_ARG
+    bad = mocatt.default_opts(exp_mode=7)
+    assert call(dp.c_struct(), bad) == mocatt.MOC_ERR_INVALID_ARG
+    assert L.moc_attenuate_fwd(None, mocatt.C.byref(dp.c_struct()), mocatt.C.byref(o),
+                               None) == mocatt.MOC_ERR_INVALID_ARG
+
+
+def test_sweep_50M_g128_track_subset_and_tally_split(handle):
+    """Full-size workload (50M segments x 128 groups). psi of a track depends only on
+    its own segments, so a sample of tracks run alone through the oracle pins psi; the
+    tallies are checked by linearity: all tracks minus the rest equals the sample."""
+    import torch
+
+    hp = mocatt.generate(mocatt.WORKLOADS["sweep_50M_g128"])
+    dp = mocatt.DeviceProblem(hp)
+    handle.fwd(dp)
+    assert handle.synchronize() == 0
+    psi = dp.to_host("psi")
+    ff_all = dp.to_host("fine_flux")
+    del dp
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(7)
+    sample = np.sort(rng.choice(hp.T, 64, replace=False))
+    sub = hp.subset_tracks(sample)
+    ref = oracle.fwd_fp64(sub)
+    rp = parity.ratio(psi[sample, :hp.G], ref["psi"][:, :hp.G], parity.bound_psi(ref, hp.G))
+    assert rp.max() <= 1.0, rp.max()
+    rest = hp.subset_tracks(np.setdiff1d(np.arange(hp.T), sample))
+    dp2 = mocatt.DeviceProblem(rest)
+    handle.fwd(dp2)
+    assert handle.synchronize() == 0
+    ff_rest = dp2.to_host("fine_flux")
+    diff = ff_all[:, :hp.G].astype(np.float64) - ff_rest[:, :hp.G]
+    # each full-size cell sums ~1,000 tallies: bound by the FP32 summation of both sums
+    tol = parity.U32 * 2048 * np.abs(ff_all[:, :hp.G]) + parity.bound_ff(ref, hp.G)
+    assert np.all(np.abs(diff - ref["ff"][:, :hp.G]) <= tol)
