@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 segment-attenuation sweep: prints ONE JSON line on rank 0.
+
+A step is one forward sweep (moc_attenuate_fwd) over the whole workload: every segment
+of every track, every energy group. The default workload is the reference's default
+problem size (-s 50000000 -e 128): 50,000,000 segments x 128 groups, 100,000 tracks,
+10,000 regions x 5 fine axial intervals, seeded synthetic inputs (the reference reads
+no dataset; it draws random inputs itself).
+
+  value        segment*group attenuations per second, inputs resident in HBM, CUDA
+               events around each sweep call on the launching stream, L2 flushed
+               (256 MiB write) between steps
+  e2e          the same metric through moc_attenuate_fwd_host on page-locked host
+               arrays: every step copies all inputs in and psi + fine_flux out
+  roofline     the sweep kernel against its binding resource (L2: row gathers +
+               tally reductions), with the HBM fraction beside it
+  cpu_baseline the reference sweep restated in C (OpenMP over tracks, per-cell locks,
+               the reference's gnu flags), on a bounded sample of the same workload
+
+--impl reference times that CPU reference arm alone (all host threads), as the
+reference's own path for this workload.
+--peaks runs the roofline microbenchmarks and writes profiles/peaks_gb300.json.
+
+Multi-GPU: the sweep runs on one GPU; with torchrun every rank runs its own replica of
+the workload (no collective in the data path) and the slowest rank sets the time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "simplemoc-kernel_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "segment·group attenuations/s, plain FP32 vs chosen form at ≤1e-5 rel err, %HBM"
+UNIT = "segment·group attenuations/s"
+PEAKS_FILE = os.path.join(ROOT, "profiles", "peaks_gb300.json")
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+# Algorithmic L2 bytes per segment*group of the plain FP32 sweep at G=128, I=5:
+# sigT row 4 B + axial-coefficient rows (3 rows for interior intervals, 2 at the ends:
+# (3*3 + 2*2)/5 * 4 B = 10.4 B) + tally reduction 4 B + descriptor 9 B / 128 groups.
+def l2_bytes_per_unit(I: int, G: int) -> dict:
+    rows = (3 * (I - 2) + 2 * 2) / I
+    return {"gather": 4.0 + 4.0 * rows + 9.0 / G, "reduce": 4.0}
+
+
+def hbm_compulsory_bytes(hp) -> float:
+    """Bytes a sweep must move to or from HBM at least once: descriptors, offsets, psi in
+    and out, sigT, source (read by the coefficient pass), coefficients written and read,
+    fine_flux read and written."""
+    S, T, Gs, R, I = hp.S, hp.T, hp.Gs, hp.R, hp.I
+    return (9.0 * S + 8.0 * (T + 1) + 2 * 4.0 * T * Gs + 4.0 * R * Gs + 4.0 * R * I * Gs
+            + 2 * 12.0 * R * I * Gs + 2 * 4.0 * R * I * Gs)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(workload, sample_tracks: int, steps: int, warmup: int,
+                 table_points: int = 0) -> dict:
+    """The CPU reference arm (oracle/_build/cpu_bench) on a bounded sample."""
+    exe = os.path.join(ROOT, "oracle", "_build", "cpu_bench")
+    if not os.path.exists(exe):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    args = [exe] + workload.cpu_bench_args() + [
+        "--sample-tracks", str(sample_tracks), "--steps", str(steps), "--warmup", str(warmup)]
+    if table_points:
+        args += ["--table", str(table_points), "10.0"]
+    out = subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    r = json.loads(out.strip().splitlines()[-1])
+    r["sample"] = (f"first {r['sample_tracks']} of {workload.tracks} tracks "
+                   f"({r['sample_segments']} segments x {r['groups']} groups), "
+                   f"{steps} timed passes after {warmup} warm-up")
+    return r
+
+
+def load_peaks() -> dict:
+    peaks = {}
+    if os.path.exists(MEASURED_PEAKS):
+        with open(MEASURED_PEAKS) as f:
+            m = json.load(f)
+        peaks["hbm_gbs"] = m.get("hbm_gbs")
+        peaks["hbm_source"] = "MEASURED_PEAKS.json (measured copy bandwidth)"
+    else:
+        peaks["hbm_gbs"] = 6800.0
+        peaks["hbm_source"] = "fallback 6.8 TB/s"
+    if os.path.exists(PEAKS_FILE):
+        with open(PEAKS_FILE) as f:
+            peaks.update(json.load(f))
+    return peaks
+
+
+def run_peaks() -> dict:
+    lib = C.CDLL(os.path.join(PKG, "_build", "libmocpeaks.so"))
+    lib.mocpeak_run.restype = C.c_int
+    res = (C.c_double * 6)()
+    rc = lib.mocpeak_run(res, 6)
+    if rc:
+        raise RuntimeError(f"mocpeak_run failed: {rc}")
+    out = {"l2_stream_read_gbs": res[0], "l2_row_gather_gbs": res[1],
+           "l2_row_reduce_gbs": res[2], "fp32_fma_tflops": res[3], "mufu_ex2_gops": res[4],
+           "hbm_read_gbs": res[5],
+           "how": "simplemoc-kernel_gb300/csrc/moc_peaks.cu via bench.py --peaks: "
+                  "CUDA events, mean of 5 launches after 1 warm-up"}
+    return out
+
+
+def reference_arm(args, workload):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    r = cpu_baseline(workload, args.cpu_sample_tracks, args.steps, args.warmup,
+                     args.table_points if args.exp == "table" else 0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["s_per_step"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 generator, same inputs as the GPU arm)",
+        "config": config_of(args, workload),
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"],
+                         "kind": "port", "sample": r["sample"], "compiler": r["compiler"]},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, w) -> dict:
+    return {"workload": w.name, "segments": w.segments, "groups": w.groups,
+            "tracks": w.tracks, "regions": w.regions, "intervals": w.intervals,
+            "exp_mode": args.exp, "form": "plain FP32 (reference computation, drop-in)",
+            "l2": "flushed between steps (256 MiB write); 0.5 GB of descriptors per step "
+                  "exceeds L2", "parallelism": "replicas only (one sweep per GPU)"}
+
+
+def gpu_arm(args, workload):
+    import numpy as np
+    import torch
+
+    import mocatt
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    hp = mocatt.generate(workload)
+    dp = mocatt.DeviceProblem(hp, dev)
+    h = mocatt.Handle(local)
+    kw = dict(profile=1)
+    if args.exp == "table":
+        kw.update(exp_mode=mocatt.MOC_EXP_TABLE, table_points=args.table_points, table_max=10.0)
+    opts = mocatt.default_opts(**kw)
+    stream = torch.cuda.current_stream(dev)
+    units = float(hp.S) * hp.G
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        h.fwd(dp, opts, stream)
+    torch.cuda.synchronize(dev)
+    if h.synchronize(stream):
+        raise RuntimeError("device error during warm-up")
+
+    gpu_index = local
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis and vis.split(",")[local].strip().isdigit():
+        gpu_index = int(vis.split(",")[local])
+    clocks = ClockSampler(gpu_index)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    step_ms, sweep_ms, prep_ms = [], [], []
+    launches = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.fwd(dp, opts, stream)
+        e1.record(stream)
+        t = h.timings()  # waits for this step's kernels
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        sweep_ms.append(t.sweep_ms)
+        prep_ms.append(t.prep_ms)
+        launches += t.launches
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    if h.synchronize(stream):
+        raise RuntimeError("device error during the timed steps")
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = ws * units * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the host entry point, page-locked host arrays ----------
+    pinned = hp.copy()
+    for name in mocatt.DeviceProblem.NAMES:
+        a = getattr(hp, name)
+        t_ = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        setattr(pinned, name, t_.numpy())
+    h2d = sum(getattr(pinned, n).nbytes for n in mocatt.DeviceProblem.NAMES)
+    d2h = pinned.psi.nbytes + pinned.fine_flux.nbytes
+    e2e_steps = max(1, min(args.steps, 5))
+    h.fwd_host(pinned, opts)  # warm-up (sizes the device copies once)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.fwd_host(pinned, opts)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": ws * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+           "call": "moc_attenuate_fwd_host (copies in, sweep, copies out, returns synced)"}
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the sweep kernel ----------------------------------------------
+    peaks = load_peaks()
+    sweep_s = statistics.mean(sweep_ms) * 1e-3
+    per = l2_bytes_per_unit(hp.I, hp.G)
+    l2_bytes = (per["gather"] + per["reduce"]) * units
+    roof = {"bound": "l2", "unit": "GB/s",
+            "achieved": l2_bytes / sweep_s / 1e9,
+            "algorithmic_bytes_per_unit": per["gather"] + per["reduce"],
+            "units_per_launch": units, "sweep_ms": sweep_s * 1e3,
+            "prep_ms": statistics.mean(prep_ms), "traffic": None}
+    if "l2_row_gather_gbs" in peaks:
+        t_l2 = (per["gather"] * units / (peaks["l2_row_gather_gbs"] * 1e9) +
+                per["reduce"] * units / (peaks["l2_row_reduce_gbs"] * 1e9))
+        roof["peak"] = l2_bytes / t_l2 / 1e9
+        roof["peak_source"] = ("profiles/peaks_gb300.json: random 512-byte row gathers and "
+                               "red.v4 row reductions into L2-resident tables, combined in "
+                               "the sweep's byte mix")
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        terms = {"l2": t_l2 * 1e3,
+                 "mufu": 2 * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3,
+                 "fp32": 34 * units / (peaks["fp32_fma_tflops"] * 1e12 / 2) * 1e3}
+    else:
+        roof["peak"] = None
+        roof["frac"] = None
+        terms = {}
+    hbm_bytes = hbm_compulsory_bytes(hp)
+    terms["hbm"] = hbm_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
+    roof["terms_ms"] = terms
+    roof["hbm"] = {"compulsory_bytes": hbm_bytes, "achieved_gbs": hbm_bytes / sweep_s / 1e9,
+                   "peak_gbs": peaks["hbm_gbs"], "frac": hbm_bytes / sweep_s / 1e9 / peaks["hbm_gbs"],
+                   "peak_source": peaks["hbm_source"]}
+    prof = os.path.join(ROOT, "profiles", "sweep_fwd_50M_g128_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            roof["traffic"] = json.load(f).get("dram_bytes_per_launch")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 generator; the reference draws random inputs "
+                "itself and reads no dataset)",
+        "config": config_of(args, workload), "roofline": roof, "e2e": e2e,
+        "gpu_launches": launches, "clocks": clk,
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
+                         args.table_points if args.exp == "table" else 0)
+        line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": r["cores"],
+                                "kind": "port", "sample": r["sample"],
+                                "compiler": r["compiler"]}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--workload", default="sweep_50M_g128")
+    ap.add_argument("--exp", default="full", choices=["full", "table"])
+    ap.add_argument("--table-points", type=int, default=10_000)
+    ap.add_argument("--cpu-sample-tracks", type=int, default=20_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--peaks", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "mine" and not args.peaks:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    import mocatt
+
+    workload = mocatt.WORKLOADS[args.workload]
+    if args.peaks:
+        out = run_peaks()
+        os.makedirs(os.path.dirname(PEAKS_FILE), exist_ok=True)
+        with open(PEAKS_FILE, "w") as f:
+            json.dump(out, f, indent=1)
+        print(json.dumps(out))
+        return
+    if args.impl == "reference":
+        reference_arm(args, workload)
+    else:
+        gpu_arm(args, workload)
+
+
+if __name__ == "__main__":
+    main()

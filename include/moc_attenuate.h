@@ -124,9 +124,19 @@ typedef struct {
                                      and return MOC_ERR_BAD_INDEX without touching
                                      fine_flux or psi                                     */
     int32_t vec;                  /* groups per lane: 0 = auto, else 1, 2 or 4          */
-    int32_t warps_per_block;      /* 0 = auto, else 1..32                               */
-    int32_t reserved[4];
+    int32_t warps_per_block;      /* 0 = auto, else 1..8                                */
+    int32_t profile;              /* 1: time each kernel of the call with CUDA events on
+                                     the call's stream (read with moc_last_timings)      */
+    int32_t reserved[3];
 } moc_fwd_opts_t;
+
+/* Device time of each kernel of the last call made with opts.profile = 1. */
+typedef struct {
+    float prep_ms;                /* axial-coefficient pass                              */
+    float sweep_ms;               /* the sweep kernel                                    */
+    float finish_ms;              /* tally finishing pass (0 when the form has none)     */
+    int32_t launches;             /* kernels the call launched                           */
+} moc_timings_t;
 
 /* Reference defaults: FULL exp, N=353 / maxVal=10 table, FP32, atomic tallies,
  * dz=0.1 zin=0.3 weight=0.5 mu=0.9 mu2=0.3. */
@@ -177,6 +187,10 @@ moc_status_t moc_synchronize(moc_handle_t handle, void *stream);
  */
 moc_status_t moc_build_exp_table(int32_t n_points, float max_val, float *values,
                                  float *dx, float *lookup_max);
+
+/* Wait for the events of the last profiled call and report its kernel times. Returns
+ * MOC_ERR_INVALID_ARG if no profiled call was made on this handle. */
+moc_status_t moc_last_timings(moc_handle_t handle, moc_timings_t *timings);
 
 /* Static description of a status code. */
 const char *moc_status_string(moc_status_t status);

@@ -276,29 +276,35 @@ typedef struct {
 static expo_t expo_exact(double tau)
 {
     expo_t x;
-    x.E = exp(-tau);
-    x.e = -expm1(-tau);
     if (tau < 1.0) {
-        static const double inv[40] = {
-            0, 1, 1. / 2, 1. / 3, 1. / 4, 1. / 5, 1. / 6, 1. / 7, 1. / 8, 1. / 9, 1. / 10,
-            1. / 11, 1. / 12, 1. / 13, 1. / 14, 1. / 15, 1. / 16, 1. / 17, 1. / 18, 1. / 19,
-            1. / 20, 1. / 21, 1. / 22, 1. / 23, 1. / 24, 1. / 25, 1. / 26, 1. / 27, 1. / 28,
-            1. / 29, 1. / 30, 1. / 31, 1. / 32, 1. / 33, 1. / 34, 1. / 35, 1. / 36, 1. / 37,
-            1. / 38, 1. / 39};
-        double term = tau, s2 = 0.0, s3 = 0.0, s4 = 0.0;
-        const double stop = 1e-18 * tau * tau * tau * tau / 24.0;
-        for (int k = 2; k < 40; k++) {
-            term *= tau * inv[k];
-            const double st = (k & 1) ? -term : term;
-            s2 += st;
-            if (k >= 3) s3 += st;
-            if (k >= 4) s4 += st;
-            if (k >= 4 && term < stop) break;
-        }
+        /* s4 = sum_{k=4}^{22} (-1)^k tau^k / k! by Horner in -tau (the first omitted term
+         * is below 1e-20 of s4 for tau < 1; the sum alternates with shrinking terms, so
+         * it does not cancel) */
+        static const double inv_fact[23] = {  /* 1/k!, k = 0..22, rounded to double */
+            1.0, 1.0, 0.5, 0.16666666666666666,
+            0.041666666666666664, 0.008333333333333333, 0.001388888888888889,
+            0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06,
+            2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09,
+            1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13,
+            4.779477332387385e-14, 2.8114572543455206e-15, 1.5619206968586225e-16,
+            8.22063524662433e-18, 4.110317623312165e-19, 1.9572941063391263e-20,
+            8.896791392450574e-22};
+        double h = inv_fact[22];
+        for (int k = 21; k >= 4; k--) h = h * -tau + inv_fact[k];
+        const double t2 = tau * tau, t3 = t2 * tau;
+        const double s4 = h * t2 * t2;
+        const double s3 = s4 - t3 * inv_fact[3];
+        const double s2 = s3 + t2 * inv_fact[2];
         x.tme = s2;
         x.cub = 6.0 * s4;
         x.dcub = -6.0 * s3;
+        /* e = tau - (tau - e) keeps full relative accuracy (tau - e <= tau^2/2), and
+         * E = 1 - e does too while e < 1 - 1/e_Napier */
+        x.e = tau - s2;
+        x.E = 1.0 - x.e;
     } else {
+        x.E = exp(-tau);
+        x.e = 1.0 - x.E;
         x.tme = tau - x.e;
         x.cub = tau * (tau * (tau - 3.0) + 6.0) - 6.0 * x.e;
         x.dcub = 3.0 * tau * tau - 6.0 * tau + 6.0 - 6.0 * x.E;
@@ -458,23 +464,25 @@ int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi
                     const expo_t x = c.tab.values
                                          ? expo_table(&c.tab, (float)s * (float)ds, tau)
                                          : expo_exact(tau);
-                    const double s2 = s * s, s3 = s2 * s, s4 = s2 * s2;
-                    const double reuse = tau * (tau - 2.0) + 2.0 * x.e / s3;
-                    const double fi = q[0] * x.tme / s2 + psi[g] * x.e / s +
-                                      q[1] * c.mu * reuse +
-                                      q[2] * c.mu2 * x.cub / (3.0 * s4);
-                    const double pn = q[0] * x.e / s + q[1] * c.mu * x.tme / s2 +
+                    /* reciprocal powers of s (one division; double rounding of 1/s^k is
+                     * far below the FP32 errors this oracle measures) */
+                    const double r1 = 1.0 / s, r2 = r1 * r1, r3 = r2 * r1;
+                    const double r4_3 = r2 * r2 * (1.0 / 3.0);
+                    const double reuse = tau * (tau - 2.0) + 2.0 * x.e * r3;
+                    const double fi = q[0] * x.tme * r2 + psi[g] * x.e * r1 +
+                                      q[1] * c.mu * reuse + q[2] * c.mu2 * x.cub * r4_3;
+                    const double pn = q[0] * x.e * r1 + q[1] * c.mu * x.tme * r2 +
                                       q[2] * c.mu2 * reuse + psi[g] * x.E;
                     /* error magnitudes (see oracle.h); em bounds |e| plus its absolute
                      * evaluation error (1 - expf(-tau) is off by ~2^-24 absolutely) */
                     const double em = 1.0 + fabs(x.e);
-                    const double areuse = tau * (tau + 2.0) + 2.0 * em / s3;
-                    const double afi = (aq[0] * tau + (s * fabs(psi[g]) + aq[0]) * em) / s2 +
-                                       apsi[g] * fabs(x.e) / s + aq[1] * c.mu * areuse +
+                    const double areuse = tau * (tau + 2.0) + 2.0 * em * r3;
+                    const double afi = (aq[0] * tau + (s * fabs(psi[g]) + aq[0]) * em) * r2 +
+                                       apsi[g] * fabs(x.e) * r1 + aq[1] * c.mu * areuse +
                                        aq[2] * c.mu2 *
                                            (tau * tau * tau + 3.0 * tau * tau + 6.0 * tau +
-                                            6.0 * em) / (3.0 * s4);
-                    const double apn = aq[0] * em / s + aq[1] * c.mu * (tau + em) / s2 +
+                                            6.0 * em) * r4_3;
+                    const double apn = aq[0] * em * r1 + aq[1] * c.mu * (tau + em) * r2 +
                                        aq[2] * c.mu2 * areuse +
                                        fabs(psi[g]) * (x.E + em) + apsi[g] * x.E;
                     tl[g] = c.weight * fi;

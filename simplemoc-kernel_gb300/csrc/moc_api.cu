@@ -26,6 +26,10 @@ struct moc_handle_s {
     void *hbuf[8] = {};
     size_t hcap[8] = {};
     cudaStream_t hstream = nullptr;
+    // kernel timing of the last profiled call
+    cudaEvent_t ev[4] = {};
+    int timed_launches = 0;   // 0: no profiled call yet
+    bool timed_finish = false;
     std::string last_error;
 };
 
@@ -196,10 +200,20 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
 
+    const bool prof = o->profile != 0;
+    if (prof && !h->ev[0])
+        for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
     MOC_CUDA(h, moc::launch_prep_coef(p->source, h->coef, p->n_regions, p->n_intervals,
                                       p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));
     MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st));
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     MOC_CUDA(h, moc::launch_fwd(sp, cfg, st));
+    if (prof) {
+        MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
+        h->timed_launches = 2;
+        h->timed_finish = false;
+    }
     return MOC_OK;
 }
 
@@ -267,6 +281,8 @@ moc_status_t moc_destroy(moc_handle_t h)
     for (int k = 0; k < 8; k++)
         if (h->hbuf[k]) cudaFree(h->hbuf[k]);
     if (h->hstream) cudaStreamDestroy(h->hstream);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
     delete h;
     return MOC_OK;
 }
@@ -356,6 +372,23 @@ moc_status_t moc_build_exp_table(int32_t n_points, float max_val, float *values,
     }
     *dx = d;
     *lookup_max = max_val - d;
+    return MOC_OK;
+}
+
+moc_status_t moc_last_timings(moc_handle_t h, moc_timings_t *t)
+{
+    if (!h || !t || h->timed_launches == 0) return MOC_ERR_INVALID_ARG;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    const cudaEvent_t last = h->timed_finish ? h->ev[3] : h->ev[2];
+    MOC_CUDA(h, cudaEventSynchronize(last));
+    float a = 0, b = 0, c = 0;
+    MOC_CUDA(h, cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
+    MOC_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
+    if (h->timed_finish) MOC_CUDA(h, cudaEventElapsedTime(&c, h->ev[2], h->ev[3]));
+    t->prep_ms = a;
+    t->sweep_ms = b;
+    t->finish_ms = c;
+    t->launches = h->timed_launches;
     return MOC_OK;
 }
 

@@ -1,0 +1,167 @@
+// moc_peaks.cu — microbenchmarks for the roofline of the sweep (libmocpeaks.so).
+//
+// The sweep is not bound by HBM or tensor cores but by L2 (row gathers and tally
+// reductions into L2-resident tables) and by FP32/MUFU issue. None of those peaks is in
+// the measured set, so this file measures them on the GPU at hand:
+//   [0] L2 streaming read GB/s   float4 __ldcg over a 64 MiB buffer, many passes
+//   [1] L2 row-gather GB/s       one random 512-byte row per warp from a 96 MiB table
+//                                (the sweep's sigT / coefficient row pattern)
+//   [2] L2 vector-reduction GB/s red.global.add.v4.f32 of random 512-byte rows into a
+//                                25.6 MB array (the sweep's tally pattern), 16 B/lane
+//   [3] FP32 FMA TFLOP/s         independent FMA chains, 2 flops each
+//   [4] MUFU ex2 Gop/s           ex2.approx chains
+//   [5] HBM read GB/s            float4 __ldcs over a 2 GiB buffer
+// Every index is taken modulo its buffer; no kernel waits on anything.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace {
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+__global__ void stream_read(const float4 *__restrict__ buf, int64_t n4, int passes, float *out,
+                            int streaming)
+{
+    const int64_t T = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float acc = 0.0f;
+    for (int p = 0; p < passes; p++)
+        for (int64_t k = tid; k < n4; k += T) {
+            const float4 v = streaming ? __ldcs(buf + k) : __ldcg(buf + k);
+            acc += v.x + v.y + v.z + v.w;
+        }
+    if (acc == 1234.5f) out[tid] = acc;  // keeps the loads alive
+}
+
+__global__ void row_gather(const float4 *__restrict__ rows, uint32_t n_rows, int iters,
+                           float *out)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    float acc = 0.0f;
+    for (int i = 0; i < iters; i++) {
+        const uint32_t r = hash32(warp * 7919u + (uint32_t)i) % n_rows;
+        const float4 v = __ldg(rows + (int64_t)r * 32 + lane);
+        acc += v.x + v.y + v.z + v.w;
+    }
+    if (acc == 1234.5f) out[warp] = acc;
+}
+
+__global__ void row_reduce(float *ff, uint32_t n_rows, int iters)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int i = 0; i < iters; i++) {
+        const uint32_t r = hash32(warp * 104729u + (uint32_t)i) % n_rows;
+        float *p = ff + (int64_t)r * 128 + lane * 4;
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(1.0f),
+                     "f"(1.0f), "f"(1.0f), "f"(1.0f)
+                     : "memory");
+    }
+}
+
+__global__ void fma_chains(float *out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+        x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+    }
+    const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void ex2_chains(float *out, int iters)
+{
+    float x0 = threadIdx.x * 1e-3f, x1 = x0 + 0.1f, x2 = x0 + 0.2f, x3 = x0 + 0.3f;
+    for (int i = 0; i < iters; i++) {
+        asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(x0));
+        asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(x1));
+        asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(x2));
+        asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(x3));
+    }
+    const float s = x0 + x1 + x2 + x3;
+    if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename F>
+float time_ms(F launch, int reps)
+{
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    launch();  // warm-up
+    cudaEventRecord(a);
+    for (int r = 0; r < reps; r++) launch();
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+}
+
+}  // namespace
+
+extern "C" int mocpeak_run(double *res, int n_res)
+{
+    if (!res || n_res < 6) return -1;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const int blocks = sms * 8, threads = 256;
+    float *out = nullptr, *l2buf = nullptr, *rows = nullptr, *ff = nullptr, *hbm = nullptr;
+    const int64_t l2_bytes = 64ll << 20, row_bytes = 96ll << 20, ff_rows = 50000,
+                  hbm_bytes = 2ll << 30;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)) != cudaSuccess) return -2;
+    if (cudaMalloc(&l2buf, l2_bytes) != cudaSuccess) return -2;
+    if (cudaMalloc(&rows, row_bytes) != cudaSuccess) return -2;
+    if (cudaMalloc(&ff, ff_rows * 128 * sizeof(float)) != cudaSuccess) return -2;
+    if (cudaMalloc(&hbm, hbm_bytes) != cudaSuccess) return -2;
+    cudaMemset(l2buf, 0, l2_bytes);
+    cudaMemset(rows, 0, row_bytes);
+    cudaMemset(ff, 0, ff_rows * 128 * sizeof(float));
+    cudaMemset(hbm, 0, hbm_bytes);
+
+    const int64_t n4 = l2_bytes / 16;
+    const int passes = 20;
+    float ms = time_ms([&] { stream_read<<<blocks, threads>>>((const float4 *)l2buf, n4, passes, out, 0); }, 5);
+    res[0] = (double)l2_bytes * passes / (ms * 1e-3) / 1e9;
+
+    const uint32_t n_rows = (uint32_t)(row_bytes / 512);
+    const int giters = 2000;
+    ms = time_ms([&] { row_gather<<<blocks, threads>>>((const float4 *)rows, n_rows, giters, out); }, 5);
+    res[1] = (double)blocks * (threads / 32) * giters * 512.0 / (ms * 1e-3) / 1e9;
+
+    const int riters = 1000;
+    ms = time_ms([&] { row_reduce<<<blocks, threads>>>(ff, (uint32_t)ff_rows, riters); }, 5);
+    res[2] = (double)blocks * (threads / 32) * riters * 512.0 / (ms * 1e-3) / 1e9;
+
+    const int fiters = 20000;
+    ms = time_ms([&] { fma_chains<<<blocks, threads>>>(out, fiters, 0.999f, 1e-3f); }, 5);
+    res[3] = (double)blocks * threads * fiters * 8 * 2.0 / (ms * 1e-3) / 1e12;
+
+    const int eiters = 5000;
+    ms = time_ms([&] { ex2_chains<<<blocks, threads>>>(out, eiters); }, 5);
+    res[4] = (double)blocks * threads * eiters * 4.0 / (ms * 1e-3) / 1e9;
+
+    ms = time_ms([&] { stream_read<<<blocks, threads>>>((const float4 *)hbm, hbm_bytes / 16, 1, out, 1); }, 5);
+    res[5] = (double)hbm_bytes / (ms * 1e-3) / 1e9;
+
+    const cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(out);
+    cudaFree(l2buf);
+    cudaFree(rows);
+    cudaFree(ff);
+    cudaFree(hbm);
+    return e == cudaSuccess ? 0 : -3;
+}

@@ -62,8 +62,14 @@ class MocFwdOpts(C.Structure):
         ("precision", C.c_int), ("tally", C.c_int),
         ("dz", C.c_float), ("zin", C.c_float), ("weight", C.c_float), ("mu", C.c_float),
         ("mu2", C.c_float), ("checked", C.c_int32), ("vec", C.c_int32),
-        ("warps_per_block", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("warps_per_block", C.c_int32), ("profile", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
+
+
+class MocTimings(C.Structure):
+    _fields_ = [("prep_ms", C.c_float), ("sweep_ms", C.c_float), ("finish_ms", C.c_float),
+                ("launches", C.c_int32)]
 
 
 class SynthSpec(C.Structure):
@@ -88,6 +94,7 @@ ABI = {
     "moc_synchronize": (C.c_int, [_P, _P]),
     "moc_build_exp_table": (C.c_int, [C.c_int32, C.c_float, _P, C.POINTER(C.c_float),
                                       C.POINTER(C.c_float)]),
+    "moc_last_timings": (C.c_int, [_P, C.POINTER(MocTimings)]),
     "moc_status_string": (C.c_char_p, [C.c_int]),
     "moc_last_error": (C.c_char_p, [_P]),
     "moc_abi_version": (C.c_int32, []),
@@ -381,6 +388,11 @@ class Handle:
         opts = opts or default_opts()
         prob = hp.c_struct()
         self.check(lib().moc_attenuate_fwd_host(self._h, C.byref(prob), C.byref(opts)))
+
+    def timings(self) -> MocTimings:
+        t = MocTimings()
+        self.check(lib().moc_last_timings(self._h, C.byref(t)))
+        return t
 
     def synchronize(self, stream=None) -> int:
         import torch

@@ -2,6 +2,7 @@
 
     libmocatt.so    the C-ABI sweep library (include/moc_attenuate.h), CUDA for sm_103a
     libmocsynth.so  the seeded input generator (include/moc_synth.h), plain C
+    libmocpeaks.so  roofline microbenchmarks (L2 gather / reduction, FP32, MUFU, HBM)
 
 Objects are rebuilt only when a source or header is newer. Translation units compile in
 parallel. Host code is compiled with -ffp-contract=off so it rounds identically on x86
@@ -32,6 +33,8 @@ CU_SOURCES = ["moc_api.cu", "moc_sweep.cu"]
 
 LIB = os.path.join(BUILD, "libmocatt.so")
 SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")
+PEAKS_LIB = os.path.join(BUILD, "libmocpeaks.so")
+DRIVER = os.path.join(BUILD, "mocatt_run")  # C host program (host/moc_driver.c)
 
 
 def nvcc() -> str:
@@ -83,6 +86,10 @@ def build(verbose: bool = False) -> dict:
     if _stale(SYNTH_LIB, [synth_src, os.path.join(INCLUDE, "moc_synth.h")]):
         synth_cmd = ["gcc", "-std=gnu99", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
                      "-I" + INCLUDE, synth_src, "-o", SYNTH_LIB, "-lm"]
+    peaks_src = os.path.join(CSRC, "moc_peaks.cu")
+    if _stale(PEAKS_LIB, [peaks_src]):
+        jobs.append([nvcc()] + NVCC_FLAGS + ["-shared", "-cudart", "static", peaks_src,
+                                             "-o", PEAKS_LIB])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs) + 1)) as ex:
         futs = [ex.submit(_run, j, verbose) for j in jobs]
         if synth_cmd:
@@ -91,7 +98,13 @@ def build(verbose: bool = False) -> dict:
             f.result()
     if _stale(LIB, objs):
         _run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs, verbose)
-    return {"libmocatt": LIB, "libmocsynth": SYNTH_LIB}
+    driver_src = os.path.join(HOST, "moc_driver.c")
+    if _stale(DRIVER, [driver_src, synth_src, LIB] + hdrs):
+        _run(["gcc", "-std=gnu99", "-O2", "-ffp-contract=off", "-I" + INCLUDE, driver_src,
+              synth_src, "-L" + BUILD, "-lmocatt", "-Wl,-rpath,$ORIGIN", "-lm", "-o", DRIVER],
+             verbose)
+    return {"libmocatt": LIB, "libmocsynth": SYNTH_LIB, "libmocpeaks": PEAKS_LIB,
+            "mocatt_run": DRIVER}
 
 
 if __name__ == "__main__":
