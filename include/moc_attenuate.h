@@ -57,7 +57,9 @@ typedef enum {
     MOC_ERR_OUT_OF_MEMORY = 6,   /* workspace allocation failed                      */
     MOC_ERR_BAD_INDEX = 7,       /* checked mode: a segment named a region, interval
                                     or track offset out of range; nothing was added  */
-    MOC_ERR_DEVICE_TIMEOUT = 8   /* a bounded device-side wait gave up               */
+    MOC_ERR_DEVICE_TIMEOUT = 8,  /* a bounded device-side wait gave up               */
+    MOC_ERR_TOO_LARGE = 9        /* the problem exceeds the fixed scratch of
+                                    moc_attenuate_fwd_noalloc                         */
 } moc_status_t;
 
 typedef struct moc_handle_s *moc_handle_t;
@@ -168,6 +170,33 @@ moc_status_t moc_attenuate_fwd(moc_handle_t handle, const moc_problem_t *problem
  */
 moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *problem,
                                     const moc_fwd_opts_t *opts);
+
+/*
+ * moc_attenuate_fwd without allocating. No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc — a transport code whose own pool allocator holds
+ * the GPU's memory and forbids further allocations, a sweep loop that cannot take the
+ * device-wide synchronisation cudaMalloc/cudaFree may cause while other streams run,
+ * or a stateless call site with nowhere to keep a handle.
+ *
+ * Same sweep, same kernels and same results as moc_attenuate_fwd, on the current CUDA
+ * device, asynchronous on `stream`. Its scratch is one fixed array in the library's
+ * device image (every GPU that loads the library holds it, about 8.2 MiB, until the
+ * process exits); nothing is allocated per call: no cudaMalloc, cudaFree or allocating
+ * library routine. Limits: n_regions * n_intervals * group_stride * 3 <=
+ * MOC_NOALLOC_MAX_COEF_FLOATS and, in table mode, table_points <=
+ * MOC_NOALLOC_MAX_TABLE_POINTS; larger problems return MOC_ERR_TOO_LARGE.
+ *
+ * The first call on each device looks up the array's device address (once, with that
+ * device current); make that first call before any stream capture. Every call shares
+ * the one array, and it keeps the last call's contents: calls whose kernels overlap on
+ * the GPU race on it, so order them on one stream. Out-of-range segment indices are
+ * skipped by the kernel; with opts->checked = 1 the call validates first, waits, and
+ * returns MOC_ERR_BAD_INDEX without touching psi or fine_flux.
+ */
+#define MOC_NOALLOC_MAX_COEF_FLOATS 2097152 /* 8 MiB of axial coefficients */
+#define MOC_NOALLOC_MAX_TABLE_POINTS 24000
+moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *problem,
+                                       const moc_fwd_opts_t *opts, void *stream);
 
 /*
  * Wait for `stream`, then report and clear the device-side error word of the handle:

@@ -219,6 +219,21 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
 
 }  // namespace
 
+// Argument checks shared with the other entry points (declared in moc_internal.h).
+moc_status_t moc::check_args(const moc_problem_t *p, const moc_fwd_opts_t *o)
+{
+    return check_problem(p, o);
+}
+
+bool moc::all_device_accessible(const moc_problem_t *p)
+{
+    const void *ptrs[] = {p->track_offsets, p->seg_region, p->seg_interval, p->seg_ds,
+                          p->sigT, p->source, p->fine_flux, p->psi};
+    for (const void *q : ptrs)
+        if (!device_accessible(q)) return false;
+    return true;
+}
+
 extern "C" {
 
 void moc_fwd_opts_default(moc_fwd_opts_t *o)
@@ -404,6 +419,7 @@ const char *moc_status_string(moc_status_t s)
     case MOC_ERR_OUT_OF_MEMORY: return "out of device memory";
     case MOC_ERR_BAD_INDEX: return "segment index or track offset out of range";
     case MOC_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case MOC_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
     }
     return "unknown status";
 }

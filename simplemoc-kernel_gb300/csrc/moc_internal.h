@@ -4,7 +4,14 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "moc_attenuate.h"
+
 namespace moc {
+
+// The size / enum / alignment checks of moc_attenuate_fwd, and its check that every
+// problem pointer is device (or managed) memory.
+moc_status_t check_args(const moc_problem_t *p, const moc_fwd_opts_t *o);
+bool all_device_accessible(const moc_problem_t *p);
 
 // Device error bits, OR-ed into the handle's error word by the kernels.
 enum : int32_t {

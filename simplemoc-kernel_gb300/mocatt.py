@@ -33,6 +33,7 @@ MOC_ERR_NO_DEVICE = 5
 MOC_ERR_OUT_OF_MEMORY = 6
 MOC_ERR_BAD_INDEX = 7
 MOC_ERR_DEVICE_TIMEOUT = 8
+MOC_ERR_TOO_LARGE = 9
 
 MOC_EXP_FULL = 0
 MOC_EXP_TABLE = 1
@@ -95,6 +96,7 @@ ABI = {
     "moc_build_exp_table": (C.c_int, [C.c_int32, C.c_float, _P, C.POINTER(C.c_float),
                                       C.POINTER(C.c_float)]),
     "moc_last_timings": (C.c_int, [_P, C.POINTER(MocTimings)]),
+    "moc_attenuate_fwd_noalloc": (C.c_int, [C.POINTER(MocProblem), C.POINTER(MocFwdOpts), _P]),
     "moc_status_string": (C.c_char_p, [C.c_int]),
     "moc_last_error": (C.c_char_p, [_P]),
     "moc_abi_version": (C.c_int32, []),
