@@ -259,22 +259,24 @@ def gpu_arm(args, workload):
     value = ws * units * args.steps / (total_ms * 1e-3)
 
     # ---- end to end through the host entry point, page-locked host arrays ----------
-    pinned = hp.copy()
-    for name in mocatt.DeviceProblem.NAMES:
-        a = getattr(hp, name)
-        t_ = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-        setattr(pinned, name, t_.numpy())
-    h2d = sum(getattr(pinned, n).nbytes for n in mocatt.DeviceProblem.NAMES)
-    d2h = pinned.psi.nbytes + pinned.fine_flux.nbytes
-    e2e_steps = max(1, min(args.steps, 5))
-    h.fwd_host(pinned, opts)  # warm-up (sizes the device copies once)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        h.fwd_host(pinned, opts)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e = {"value": ws * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-           "call": "moc_attenuate_fwd_host (copies in, sweep, copies out, returns synced)"}
+    e2e = None
+    if not args.no_e2e:
+        pinned = hp.copy()
+        for name in mocatt.DeviceProblem.NAMES:
+            a = getattr(hp, name)
+            t_ = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            setattr(pinned, name, t_.numpy())
+        h2d = sum(getattr(pinned, n).nbytes for n in mocatt.DeviceProblem.NAMES)
+        d2h = pinned.psi.nbytes + pinned.fine_flux.nbytes
+        e2e_steps = max(1, min(args.steps, 5))
+        h.fwd_host(pinned, opts)  # warm-up (sizes the device copies once)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            h.fwd_host(pinned, opts)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e = {"value": ws * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+               "call": "moc_attenuate_fwd_host (copies in, sweep, copies out, returns synced)"}
 
     if rank != 0:
         if ws > 1:
@@ -348,6 +350,10 @@ def main():
     ap.add_argument("--table-points", type=int, default=10_000)
     ap.add_argument("--cpu-sample-tracks", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--segments", type=int, default=0,
+                    help="override the workload's segment count (smaller profiling cases)")
+    ap.add_argument("--tracks", type=int, default=0, help="override the track count")
     ap.add_argument("--peaks", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "mine" and not args.peaks:
@@ -356,6 +362,10 @@ def main():
     import mocatt
 
     workload = mocatt.WORKLOADS[args.workload]
+    if args.segments:
+        workload = workload.with_(segments=args.segments)
+    if args.tracks:
+        workload = workload.with_(tracks=args.tracks)
     if args.peaks:
         out = run_peaks()
         os.makedirs(os.path.dirname(PEAKS_FILE), exist_ok=True)
