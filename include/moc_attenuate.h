@@ -73,11 +73,18 @@ typedef enum {
                            reproduced exactly (including its slope sign and index rule)   */
 } moc_exp_mode_t;
 
-/* Storage precision of sigT and the axial source coefficients (math is always FP32). */
+/*
+ * Storage precision of sigT and the axial source coefficients (math is always FP32).
+ * The precision forms (all but MOC_PREC_FP32) evaluate 1 - exp(-tau), tau - (1 - exp(-tau))
+ * and the cubic of src/cpu/kernel.c:250-251 from one Taylor sum below tau = 1, where the
+ * reference's expressions cancel, and accept every moc_tally_t. MOC_PREC_FP32 is the
+ * reference computation (drop-in) and takes MOC_TALLY_ATOMIC_FP32 only.
+ */
 typedef enum {
-    MOC_PREC_FP32 = 0,  /* plain method: the reference computation in FP32 (drop-in)     */
-    MOC_PREC_BF16 = 1,  /* precision form: bf16 storage, stable small-tau math           */
-    MOC_PREC_FP16 = 2   /* precision form: fp16 storage, stable small-tau math           */
+    MOC_PREC_FP32 = 0,       /* plain method: the reference computation in FP32          */
+    MOC_PREC_BF16 = 1,       /* precision form: sigT and coefficients stored as bf16      */
+    MOC_PREC_FP16 = 2,       /* precision form: sigT and coefficients stored as fp16      */
+    MOC_PREC_FP32_STABLE = 3 /* precision form with FP32 storage                          */
 } moc_precision_t;
 
 /* How fine_flux tallies are accumulated. */
@@ -172,19 +179,84 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *pr
                                     const moc_fwd_opts_t *opts);
 
 /*
+ * Batching form: sweep several problems (different group counts, tracks of very uneven
+ * length) in ONE persistent kernel launch. No single counterpart in the reference (its
+ * run_kernel, src/cpu/kernel.c:3-73, sweeps one problem); each problem is swept exactly
+ * as moc_attenuate_fwd would sweep it (plain form, either exp mode; opts is shared).
+ * Tracks are bucket-sorted by length on the device and consumed longest first from one
+ * work queue; problems whose G does not fill a warp are swept by sub-warps carrying
+ * several tracks each. The first call for a given set of problems (pointers and sizes)
+ * and options captures the whole sequence into a CUDA graph on the handle; later calls
+ * with the same set replay it with one cudaGraphLaunch on `stream`. At most
+ * MOC_BATCH_MAX_PROBLEMS problems, and at most 16 group ranges in total (a problem needs
+ * ceil(G / (32 * groups-per-lane)) of them). Groups per lane and warps per block come
+ * from opts->vec / opts->warps_per_block, else from moc_autotune_batch's result for this
+ * set, else 2 and 8.
+ */
+#define MOC_BATCH_MAX_PROBLEMS 8
+moc_status_t moc_attenuate_fwd_batch(moc_handle_t handle, const moc_problem_t *problems,
+                                     int32_t n_problems, const moc_fwd_opts_t *opts,
+                                     void *stream);
+
+/* Result of moc_autotune_batch. */
+typedef struct {
+    int32_t vec;                  /* chosen groups per lane (1, 2 or 4)                  */
+    int32_t warps_per_block;      /* chosen warps per block (1, 2, 4 or 8)               */
+    int32_t tracks_per_block;     /* tracks a block carries at once for the first problem */
+    float best_ms;                /* device time of one batched sweep with that choice   */
+    int32_t n_candidates;
+    int32_t candidate_vec[16];
+    int32_t candidate_warps[16];
+    float candidate_ms[16];
+} moc_tune_result_t;
+
+/*
+ * Autotuner of the batching form: times every (groups per lane in {1, 2, 4}) x
+ * (warps per block in {1, 2, 4, 8}) on the given problems, keeps the fastest for this
+ * set of problems in the handle (used by later moc_attenuate_fwd_batch calls whose opts
+ * leave vec / warps_per_block at 0), and reports all candidates. psi and fine_flux of
+ * the problems are saved before the trials and restored after them, so the call leaves
+ * them unchanged. Synchronous.
+ */
+moc_status_t moc_autotune_batch(moc_handle_t handle, const moc_problem_t *problems,
+                                int32_t n_problems, const moc_fwd_opts_t *opts, void *stream,
+                                moc_tune_result_t *result);
+
+/*
+ * Reverse-mode derivative of the sweep. No counterpart in the reference (which has no
+ * derivative): for
+ *     L = sum_{cells, g} w[c][g] * fine_flux_out[c][g] + sum_{tracks, g} v[t][g] * psi_out[t][g]
+ * with w = dL_dfine_flux ([R][I][group_stride]) and v = dL_dpsi_out ([T][group_stride]),
+ * writes dL/dsigT ([R][group_stride]), dL/dsource ([R][I][group_stride]) and dL/dpsi_in
+ * ([T][group_stride]) for the inputs in `problem` (problem->psi is the INCOMING psi and is
+ * only read; problem->fine_flux is not used). Padding entries of the outputs are not
+ * written. The derivative is that of the exact attenuation formula; exponentials are
+ * recomputed in the reverse sweep, and psi entering each segment is recorded by a first
+ * forward pass in handle workspace (4 * n_segments * group_stride bytes). opts->exp_mode
+ * must be MOC_EXP_FULL (the table is not differentiable); precision and tally options
+ * are ignored. Asynchronous on `stream`.
+ */
+moc_status_t moc_attenuate_adj(moc_handle_t handle, const moc_problem_t *problem,
+                               const moc_fwd_opts_t *opts, const float *dL_dfine_flux,
+                               const float *dL_dpsi_out, float *dL_dsigT, float *dL_dsource,
+                               float *dL_dpsi_in, void *stream);
+
+/*
  * moc_attenuate_fwd without allocating. No counterpart in the reference: it exists for
  * callers that cannot call cudaMalloc — a transport code whose own pool allocator holds
  * the GPU's memory and forbids further allocations, a sweep loop that cannot take the
  * device-wide synchronisation cudaMalloc/cudaFree may cause while other streams run,
  * or a stateless call site with nowhere to keep a handle.
  *
- * Same sweep, same kernels and same results as moc_attenuate_fwd, on the current CUDA
- * device, asynchronous on `stream`. Its scratch is one fixed array in the library's
- * device image (every GPU that loads the library holds it, about 8.2 MiB, until the
+ * Same sweep, same kernels and same results as moc_attenuate_fwd (plain form,
+ * opts->precision = MOC_PREC_FP32, either exp mode; other precisions return
+ * MOC_ERR_UNSUPPORTED), on the current CUDA device, asynchronous on `stream`. Its scratch is one fixed array in the library's
+ * device image (every GPU that loads the library holds it, about 10.2 MiB, until the
  * process exits); nothing is allocated per call: no cudaMalloc, cudaFree or allocating
- * library routine. Limits: n_regions * n_intervals * group_stride * 3 <=
- * MOC_NOALLOC_MAX_COEF_FLOATS and, in table mode, table_points <=
- * MOC_NOALLOC_MAX_TABLE_POINTS; larger problems return MOC_ERR_TOO_LARGE.
+ * library routine. Limits: n_regions * n_intervals * group_stride <=
+ * MOC_NOALLOC_MAX_CELL_GROUPS (16 bytes of scratch each) and, in table mode,
+ * table_points <= MOC_NOALLOC_MAX_TABLE_POINTS; larger problems return
+ * MOC_ERR_TOO_LARGE.
  *
  * The first call on each device looks up the array's device address (once, with that
  * device current); make that first call before any stream capture. Every call shares
@@ -193,7 +265,7 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *pr
  * skipped by the kernel; with opts->checked = 1 the call validates first, waits, and
  * returns MOC_ERR_BAD_INDEX without touching psi or fine_flux.
  */
-#define MOC_NOALLOC_MAX_COEF_FLOATS 2097152 /* 8 MiB of axial coefficients */
+#define MOC_NOALLOC_MAX_CELL_GROUPS 655360 /* 10 MiB of cell blocks */
 #define MOC_NOALLOC_MAX_TABLE_POINTS 24000
 moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *problem,
                                        const moc_fwd_opts_t *opts, void *stream);

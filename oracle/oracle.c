@@ -407,9 +407,69 @@ static double *promote(const float *x, int64_t n)
     return d;
 }
 
+/* FP32 coefficients a0 = q0, a1 = q1*mu, a2 = q2*mu2 of every cell, rounded as the
+ * reference's FP32 code rounds them (src/cpu/kernel.c:111-191 and the first product of
+ * kernel.c:250-251, 311-322). */
+int oracle_fit_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o, float *coef)
+{
+    if (!problem_ok(p, o) || !coef) return -1;
+    const float dz = o->dz, zin = o->zin, mu = o->mu, mu2 = o->mu2;
+    const int64_t Gs = p->group_stride, I = p->n_intervals;
+    for (int64_t cell = 0; cell < (int64_t)p->n_regions * I; cell++) {
+        const int i = (int)(cell % I);
+        const float *row = p->source + cell * Gs;
+        for (int64_t g = 0; g < Gs; g++) {
+            float q0 = 0, q1 = 0, q2 = 0;
+            if (g < p->n_groups) {
+                if (i == 0) {
+                    const float y2 = row[g], y3 = row[Gs + g];
+                    const float c1 = (y3 - y2) / dz;
+                    q0 = y2 + c1 * zin;
+                    q1 = c1;
+                } else if (i == I - 1) {
+                    const float y1 = row[g - Gs], y2 = row[g];
+                    const float c1 = (y2 - y1) / dz;
+                    q0 = y2 + c1 * zin;
+                    q1 = c1;
+                } else {
+                    const float y1 = row[g - Gs], y2 = row[g], y3 = row[Gs + g];
+                    const float c1 = (y1 - y3) / (2.f * dz);
+                    const float c2 = (y1 - 2.f * y2 + y3) / (2.f * dz * dz);
+                    q0 = y2 + c1 * zin + c2 * zin * zin;
+                    q1 = c1 + 2.f * c2 * zin;
+                    q2 = c2;
+                }
+            }
+            coef[(cell * 3 + 0) * Gs + g] = q0;
+            coef[(cell * 3 + 1) * Gs + g] = q1 * mu;
+            coef[(cell * 3 + 2) * Gs + g] = q2 * mu2;
+        }
+    }
+    return 0;
+}
+
+static int fwd64(const moc_problem_t *p, const moc_fwd_opts_t *o, const float *coef,
+                 double *psi_out, double *ff_out, double *a_psi, double *a_ff,
+                 double *abs_tally, int64_t *hits, int nthreads);
+
 int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi_out,
                     double *ff_out, double *a_psi, double *a_ff, double *abs_tally,
                     int64_t *hits, int nthreads)
+{
+    return fwd64(p, o, NULL, psi_out, ff_out, a_psi, a_ff, abs_tally, hits, nthreads);
+}
+
+int oracle_fwd_fp64_coef(const moc_problem_t *p, const moc_fwd_opts_t *o, const float *coef,
+                         double *psi_out, double *ff_out, double *a_psi, double *a_ff,
+                         double *abs_tally, int64_t *hits, int nthreads)
+{
+    if (!coef) return -1;
+    return fwd64(p, o, coef, psi_out, ff_out, a_psi, a_ff, abs_tally, hits, nthreads);
+}
+
+static int fwd64(const moc_problem_t *p, const moc_fwd_opts_t *o, const float *coef,
+                 double *psi_out, double *ff_out, double *a_psi, double *a_ff,
+                 double *abs_tally, int64_t *hits, int nthreads)
 {
     if (!problem_ok(p, o)) return -1;
     const int64_t Gs = p->group_stride, G = p->n_groups;
@@ -425,6 +485,15 @@ int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi
     if (!sig || !src || !ff || !aff || !atal || !nh || ctx_init(&c, p, o, sig, src)) {
         free(sig); free(src); free(ff); free(aff); free(atal); free(nh);
         return -1;
+    }
+    if (coef) {
+        /* given coefficients a0 = q0, a1 = q1*mu, a2 = q2*mu2 replace the fit */
+        const double scale[3] = {1.0, 1.0 / c.mu, 1.0 / c.mu2};
+        for (int64_t k = 0; k < ncell * 3 * Gs; k++) {
+            const int64_t kk = (k / Gs) % 3;
+            c.q[k] = (double)coef[k] * scale[kk];
+            c.aq[k] = fabs(c.q[k]);
+        }
     }
     for (int64_t k = 0; k < nff; k++) {
         ff[k] = p->fine_flux[k];

@@ -57,6 +57,17 @@ int oracle_fwd_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, double *psi
                     double *ff_out, double *a_psi, double *a_ff, double *abs_tally,
                     int64_t *hits, int nthreads);
 
+/* FP32 axial coefficients a0 = q0, a1 = q1*mu, a2 = q2*mu2 per cell ([R*I][3][Gs]),
+ * rounded as the reference's FP32 code rounds them. */
+int oracle_fit_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o, float *coef);
+
+/* oracle_fwd_fp64 with the axial coefficients given ([R*I][3][Gs], as oracle_fit_fp32
+ * lays them out) instead of fitted from p->source: the FP64 reference for a form that
+ * stores rounded coefficients, evaluated on exactly the values it stored. */
+int oracle_fwd_fp64_coef(const moc_problem_t *p, const moc_fwd_opts_t *o, const float *coef,
+                         double *psi_out, double *ff_out, double *a_psi, double *a_ff,
+                         double *abs_tally, int64_t *hits, int nthreads);
+
 /*
  * FP64 adjoint of the sweep for L = sum w . fine_flux_out + sum v . psi_out
  * (w [R][I][group_stride], v [T][group_stride]). Outputs dL/dsigT [R][group_stride],

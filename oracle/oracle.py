@@ -33,6 +33,8 @@ _SIGS = {
     "oracle_fwd_fp32_omp": (C.c_int, [_PP, _PO, C.c_int]),
     "oracle_fwd_fp64": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, _P, C.c_int]),
     "oracle_adj_fp64": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, C.c_int]),
+    "oracle_fit_fp32": (C.c_int, [_PP, _PO, _P]),
+    "oracle_fwd_fp64_coef": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, _P, _P, C.c_int]),
     "oracle_loss_fp64": (C.c_double, [_PP, _PO, _P, _P, _P, _P, _P, C.c_int32]),
 }
 
@@ -100,6 +102,61 @@ def fwd_fp64(hp: "mocatt.HostProblem", opts=None, threads: int = 0) -> dict:
                                out["ff"].ctypes.data, out["a_psi"].ctypes.data,
                                out["a_ff"].ctypes.data, out["abs_tally"].ctypes.data,
                                out["hits"].ctypes.data, threads)
+    if rc:
+        raise ValueError("oracle rejected the problem")
+    return out
+
+
+def fit_fp32(hp, opts=None) -> np.ndarray:
+    """The reference's FP32 axial coefficients (q0, q1*mu, q2*mu2), [R*I, 3, Gs]."""
+    opts = opts or mocatt.default_opts()
+    coef = np.zeros((hp.R * hp.I, 3, hp.Gs), np.float32)
+    if lib().oracle_fit_fp32(C.byref(hp.c_struct()), C.byref(opts), coef.ctypes.data):
+        raise ValueError("oracle rejected the problem")
+    return coef
+
+
+def round_bf16(x: np.ndarray) -> np.ndarray:
+    """float32 values rounded to bfloat16, to nearest even, returned as float32."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def round_fp16(x: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(x, np.float32).astype(np.float16).astype(np.float32)
+
+
+def quantized_inputs(hp, precision: int, opts=None):
+    """(problem with sigT as the form stores it, coefficients as the form stores them):
+    what a precision form computes from, for its FP64 reference."""
+    coef = fit_fp32(hp, opts)
+    q = hp.copy()
+    if precision == mocatt.MOC_PREC_BF16:
+        rnd = round_bf16
+    elif precision == mocatt.MOC_PREC_FP16:
+        rnd = round_fp16
+    else:
+        return q, coef
+    q.sigT = rnd(hp.sigT).reshape(hp.sigT.shape)
+    return q, rnd(coef).reshape(coef.shape)
+
+
+def fwd_fp64_coef(hp, coef, opts=None, threads: int = 0) -> dict:
+    """FP64 oracle on given coefficients (see oracle_fwd_fp64_coef)."""
+    opts = opts or mocatt.default_opts()
+    prob = hp.c_struct()
+    coef = np.ascontiguousarray(coef, np.float32)
+    ncell = hp.R * hp.I
+    out = {k: np.zeros(shape, np.float64) for k, shape in (
+        ("psi", (hp.T, hp.Gs)), ("ff", (ncell, hp.Gs)), ("a_psi", (hp.T, hp.Gs)),
+        ("a_ff", (ncell, hp.Gs)), ("abs_tally", (ncell, hp.Gs)))}
+    out["hits"] = np.zeros(ncell, np.int64)
+    rc = lib().oracle_fwd_fp64_coef(C.byref(prob), C.byref(opts), coef.ctypes.data,
+                                    out["psi"].ctypes.data, out["ff"].ctypes.data,
+                                    out["a_psi"].ctypes.data, out["a_ff"].ctypes.data,
+                                    out["abs_tally"].ctypes.data, out["hits"].ctypes.data,
+                                    threads)
     if rc:
         raise ValueError("oracle rejected the problem")
     return out

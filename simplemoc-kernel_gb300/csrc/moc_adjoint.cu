@@ -1,0 +1,338 @@
+// moc_adjoint.cu — reverse-mode derivative of the sweep (moc_attenuate_adj).
+//
+// For L = sum w . fine_flux_out + sum v . psi_out the gradients with respect to sigT,
+// the fine source and the incoming psi are accumulated by one reverse sweep per track.
+// Per segment and group (tau = s ds, e = 1 - exp(-tau), p = exp(-tau), tme = tau - e,
+// cub = tau(tau(tau-3)+6) - 6e, reuse = tau(tau-2) + 2e/s^3, a1 = q1 mu, a2 = q2 mu2):
+//   FI   = a0 tme/s^2 + psi e/s + a1 reuse + a2 cub/(3 s^4)         (tally / weight)
+//   psi' = a0 e/s + a1 tme/s^2 + a2 reuse + psi p
+// (src/cpu/kernel.c:233-331 with (q0 tau + (s psi - q0) e)/s^2 = q0 tme/s^2 + psi e/s).
+// With lambda = dL/dpsi' and W = weight * w[cell]:
+//   dL/ds   += lambda dpsi'/ds + W dFI/ds
+//   dL/da_k += lambda dpsi'/da_k + W dFI/da_k
+//   lambda  <- lambda p + W e/s                                       (dL/dpsi)
+// where, with D1 = tau e - 2 tme, D2 = tau p - e, D3 = tau dcub/dtau - 4 cub,
+//   dFI/ds   = a0 D1/s^3 + psi D2/s^2 + a1 dreuse/ds + a2 D3/(3 s^5)
+//   dpsi'/ds = a0 D2/s^2 + a1 D1/s^3 + a2 dreuse/ds - psi p ds
+//   dreuse/ds = (2 tau - 2) tau/s + (2 tau p - 6 e)/s^4.
+// D1, D2 and D3 cancel for small tau (D3 ~ -tau^5/20 from tau^4 terms); below tau = 1
+// they come from their Taylor sums, like the forward's stable terms. The exponentials
+// are recomputed from tau in the reverse sweep instead of being stored; psi entering
+// each segment is recorded by a first forward pass (one float per segment and group).
+#include "moc_device.cuh"
+#include "moc_internal.h"
+
+namespace moc {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Every term the reverse sweep needs, accurate for all tau >= 0.
+struct AdjTerms {
+    float e, p, tme, cub, d1, d2, d3;
+};
+
+__device__ __forceinline__ AdjTerms adj_terms(float tau)
+{
+    AdjTerms r;
+    if (tau < 1.0f) {
+        // s4 = sum_{k>=4} (-1)^k tau^k / k! (through tau^12)
+        float h = 1.0f / 479001600.0f;
+        h = fmaf(h, -tau, 1.0f / 39916800.0f);
+        h = fmaf(h, -tau, 1.0f / 3628800.0f);
+        h = fmaf(h, -tau, 1.0f / 362880.0f);
+        h = fmaf(h, -tau, 1.0f / 40320.0f);
+        h = fmaf(h, -tau, 1.0f / 5040.0f);
+        h = fmaf(h, -tau, 1.0f / 720.0f);
+        h = fmaf(h, -tau, 1.0f / 120.0f);
+        h = fmaf(h, -tau, 1.0f / 24.0f);
+        const float t2 = tau * tau, t3 = t2 * tau, t4 = t2 * t2;
+        const float s4 = h * t4;
+        r.cub = 6.0f * s4;
+        r.tme = fmaf(t2, fmaf(tau, -1.0f / 6.0f, 0.5f), s4);
+        r.e = tau - r.tme;
+        r.p = 1.0f - r.e;
+        // D1 = tau e - 2 tme = -tau^3/6 + tau^4/6 - (tau + 2) s4
+        r.d1 = fmaf(-(tau + 2.0f), s4, t3 * fmaf(tau, 1.0f / 6.0f, -1.0f / 6.0f));
+        // D2 = tau p - e = -tau^2/2 + tau^3/3 - tau^4/6 + (1 + tau) s4
+        r.d2 = fmaf(1.0f + tau, s4, t2 * fmaf(tau, fmaf(tau, -1.0f / 6.0f, 1.0f / 3.0f), -0.5f));
+        // D3 = 6 sum_{m>=5} (-1)^m (m-4) tau^m / m! = -6 tau^5 sum_j (j+1) (-tau)^j / (j+5)!
+        float d = 8.0f / 479001600.0f;             // (7+1)/12!
+        d = fmaf(d, -tau, 7.0f / 39916800.0f);
+        d = fmaf(d, -tau, 6.0f / 3628800.0f);
+        d = fmaf(d, -tau, 5.0f / 362880.0f);
+        d = fmaf(d, -tau, 4.0f / 40320.0f);
+        d = fmaf(d, -tau, 3.0f / 5040.0f);
+        d = fmaf(d, -tau, 2.0f / 720.0f);
+        d = fmaf(d, -tau, 1.0f / 120.0f);
+        r.d3 = -6.0f * d * t4 * tau;
+    } else {
+        r.p = exp_neg_rr(tau);
+        r.e = 1.0f - r.p;
+        r.tme = tau - r.e;
+        r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
+        r.d1 = fmaf(tau, r.e, -2.0f * r.tme);
+        r.d2 = fmaf(tau, r.p, -r.e);
+        const float dcub = fmaf(3.0f * tau, tau - 2.0f, 6.0f * r.e);  // 3t^2 - 6t + 6 - 6p
+        r.d3 = fmaf(tau, dcub, -4.0f * r.cub);
+    }
+    return r;
+}
+
+// psi' of one segment (stable terms), for the recording forward pass.
+template <int VEC>
+__device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VEC> &psi)
+{
+#pragma unroll
+    for (int k = 0; k < VEC; k++) {
+        const float s = b[k].x, a0 = b[k].y, a1 = b[k].z, a2 = b[k].w;
+        const float tau = s * ds;
+        const ExpTerms x = exp_terms_stable(tau);
+        const float rs = rcp_approx(s), rs2 = rs * rs;
+        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * (rs * rs2));
+        float pn = a0 * x.e * rs;
+        pn = fmaf(a1 * x.tme, rs2, pn);
+        pn = fmaf(a2, reuse, pn);
+        psi.v[k] = fmaf(psi.v[k], x.p, pn);
+    }
+}
+
+__device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t lo, int64_t hi,
+                                       int &cell, float &ds)
+{
+    cell = -1;
+    ds = 0.0f;
+    if (j >= lo && j < hi) {
+        const int r = ld_stream(P.reg + j);
+        const int iv = ld_stream(P.itv + j);
+        ds = ld_stream(P.ds + j);
+        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I)
+            cell = r * P.I + iv;
+        else
+            atomicOr(P.err, DEVERR_INDEX);
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void load4(const float4 *p, float4 (&b)[VEC])
+{
+#pragma unroll
+    for (int k = 0; k < VEC; k++) b[k] = __ldg(p + k);
+}
+
+__device__ __forceinline__ bool item_range(const SweepParams &P, int64_t item, int lane, int vec,
+                                           int &t, int &g0, int64_t &beg, int64_t &end)
+{
+    t = (int)(item / P.n_chunks);
+    const int ch = (int)(item - (int64_t)t * P.n_chunks);
+    g0 = (ch * 32 + lane) * vec;
+    beg = P.off[t];
+    end = P.off[t + 1];
+    if (!(beg >= 0 && beg <= end && end <= P.S)) {
+        if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
+        return false;
+    }
+    return true;
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
+{
+    const SweepParams &P = A.fw;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(P.counter, 1ULL);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= (unsigned long long)P.n_items) break;
+        int t, g0;
+        int64_t beg, end;
+        if (!item_range(P, (int64_t)item, lane, VEC, t, g0, beg, end)) continue;
+        const int nvalid = P.G - g0;
+        const bool act = nvalid > 0;
+        const int Gs = P.Gs;
+        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        Vec<VEC> psi;
+        if (act) psi = ld_psi<VEC>(P.psi + (int64_t)t * Gs + g0, nvalid);
+        for (int64_t wb = beg; wb < end; wb += 32) {
+            int cw;
+            float dw;
+            decode(P, wb + lane, beg, end, cw, dw);
+            const int n = end - wb < 32 ? (int)(end - wb) : 32;
+            for (int k = 0; k < n; k++) {
+                const int c = __shfl_sync(FULL, cw, k);
+                const float d = __shfl_sync(FULL, dw, k);
+                if (!act) continue;
+                st_psi<VEC>(A.hist + (wb + k) * Gs + g0, psi, nvalid);
+                if (c < 0) continue;
+                float4 b[VEC];
+                load4<VEC>(bb + c * Gs, b);
+                advance<VEC>(b, d, psi);
+            }
+        }
+    }
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
+{
+    const SweepParams &P = A.fw;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(P.counter, 1ULL);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= (unsigned long long)P.n_items) break;
+        int t, g0;
+        int64_t beg, end;
+        if (!item_range(P, (int64_t)item, lane, VEC, t, g0, beg, end)) continue;
+        const int nvalid = P.G - g0;
+        const bool act = nvalid > 0;
+        const int Gs = P.Gs;
+        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        Vec<VEC> lam;
+        if (act) lam = ld_psi<VEC>(A.v + (int64_t)t * Gs + g0, nvalid);
+        // windows from the end: lane l holds segment we - 32 + l
+        for (int64_t we = end; we > beg; we -= 32) {
+            int cw;
+            float dw;
+            decode(P, we - 32 + lane, beg, end, cw, dw);
+            const int n = we - beg < 32 ? (int)(we - beg) : 32;
+            for (int k = 31; k >= 32 - n; k--) {
+                const int c = __shfl_sync(FULL, cw, k);
+                const float d = __shfl_sync(FULL, dw, k);
+                if (!act || c < 0) continue;
+                const int64_t j = we - 32 + k;
+                float4 b[VEC];
+                load4<VEC>(bb + c * Gs, b);
+                const Vec<VEC> psi = ld_psi<VEC>(A.hist + j * Gs + g0, nvalid);
+                const Vec<VEC> wv = ld_psi<VEC>(A.w + c * Gs + g0, nvalid);
+#pragma unroll
+                for (int q = 0; q < VEC; q++) {
+                    const float s = b[q].x, a0 = b[q].y, a1 = b[q].z, a2 = b[q].w;
+                    const float ps = psi.v[q], la = lam.v[q], W = P.weight * wv.v[q];
+                    const float tau = s * d;
+                    const AdjTerms x = adj_terms(tau);
+                    const float rs = rcp_approx(s), rs2 = rs * rs, rs3 = rs2 * rs;
+                    const float rs4 = rs2 * rs2, rs5 = rs4 * rs;
+                    const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * rs3);
+                    const float dreuse = fmaf((2.0f * tau - 2.0f) * tau, rs,
+                                              fmaf(2.0f * tau, x.p, -6.0f * x.e) * rs4);
+                    const float fi_s = a0 * x.d1 * rs3 + ps * x.d2 * rs2 + a1 * dreuse +
+                                       a2 * x.d3 * rs5 * (1.0f / 3.0f);
+                    const float pn_s = a0 * x.d2 * rs2 + a1 * x.d1 * rs3 + a2 * dreuse -
+                                       ps * x.p * d;
+                    float4 gr;
+                    gr.x = fmaf(la, pn_s, W * fi_s);
+                    gr.y = fmaf(la, x.e * rs, W * x.tme * rs2);
+                    gr.z = fmaf(la, x.tme * rs2, W * reuse);
+                    gr.w = fmaf(la, reuse, W * x.cub * rs4 * (1.0f / 3.0f));
+                    lam.v[q] = fmaf(la, x.p, W * x.e * rs);
+                    if (q < nvalid) {
+                        float *g = reinterpret_cast<float *>(A.gblk + c * Gs + g0 + q);
+                        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(g),
+                                     "f"(gr.x), "f"(gr.y), "f"(gr.z), "f"(gr.w)
+                                     : "memory");
+                    }
+                }
+            }
+        }
+        if (act) st_psi<VEC>(A.dpsi_in + (int64_t)t * Gs + g0, lam, nvalid);
+    }
+}
+
+struct Jac {
+    float a[27];
+};
+
+__global__ void adj_finish_kernel(const float4 *__restrict__ gblk, float *__restrict__ d_sigT,
+                                  float *__restrict__ d_source, int R, int I, int G, int Gs,
+                                  Jac jac, float mu, float mu2)
+{
+    const int64_t n = (int64_t)R * Gs;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k / Gs;
+        const int g = (int)(k - r * Gs);
+        if (g >= G) continue;
+        const float4 *cb = gblk + r * I * Gs + g;
+        float ds = 0.0f;
+        for (int i = 0; i < I; i++) ds += cb[(int64_t)i * Gs].x;
+        d_sigT[r * Gs + g] = ds;
+        // source interval y of region r: every cell i with |i - y| <= 1 whose fit uses it
+        for (int y = 0; y < I; y++) {
+            float acc = 0.0f;
+            for (int i = y - 1; i <= y + 1; i++) {
+                if (i < 0 || i >= I) continue;
+                const int type = i == 0 ? 0 : (i == I - 1 ? 2 : 1);
+                const int m = y - i + 1;
+                const float4 gq = cb[(int64_t)i * Gs];
+                const float dq[3] = {gq.y, gq.z * mu, gq.w * mu2};
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) acc = fmaf(jac.a[(type * 3 + kk) * 3 + m], dq[kk], acc);
+            }
+            d_source[(r * I + y) * Gs + g] = acc;
+        }
+    }
+}
+
+template <int VEC>
+const void *fwd_fn() { return reinterpret_cast<const void *>(&adj_forward_kernel<VEC>); }
+template <int VEC>
+const void *rev_fn() { return reinterpret_cast<const void *>(&adj_reverse_kernel<VEC>); }
+
+const void *pick(int vec, bool reverse)
+{
+    if (vec == 1) return reverse ? rev_fn<1>() : fwd_fn<1>();
+    if (vec == 2) return reverse ? rev_fn<2>() : fwd_fn<2>();
+    if (vec == 4) return reverse ? rev_fn<4>() : fwd_fn<4>();
+    return nullptr;
+}
+
+cudaError_t launch(const AdjParams &p, int vec, int blocks, bool reverse, cudaStream_t st)
+{
+    const void *fn = pick(vec, reverse);
+    if (!fn || blocks < 1) return cudaErrorInvalidValue;
+    AdjParams copy = p;
+    void *args[] = {&copy};
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(256), args, 0, st);
+}
+
+}  // namespace
+
+int adj_blocks_per_sm(int vec, bool reverse)
+{
+    const void *fn = pick(vec, reverse);
+    int n = 0;
+    if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 256, 0) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_adj_forward(const AdjParams &p, int vec, int blocks, cudaStream_t st)
+{
+    return launch(p, vec, blocks, false, st);
+}
+
+cudaError_t launch_adj_reverse(const AdjParams &p, int vec, int blocks, cudaStream_t st)
+{
+    return launch(p, vec, blocks, true, st);
+}
+
+cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,
+                              int G, int Gs, const float *jac27, float mu, float mu2,
+                              cudaStream_t st)
+{
+    Jac j;
+    for (int k = 0; k < 27; k++) j.a[k] = jac27[k];
+    const int64_t n = (int64_t)R * Gs;
+    if (n == 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    adj_finish_kernel<<<(int)blocks, 256, 0, st>>>(gblk, d_sigT, d_source, R, I, G, Gs, j, mu,
+                                                   mu2);
+    return cudaGetLastError();
+}
+
+}  // namespace moc

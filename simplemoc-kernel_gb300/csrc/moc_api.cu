@@ -8,14 +8,37 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 struct moc_handle_s {
     int device = 0;
     int sm_count = 0;
     size_t l2_bytes = 0;
     // workspace (device)
-    float *coef = nullptr;
-    size_t coef_cap = 0;  // floats
+    float4 *blk = nullptr;     // cell blocks (sigT, q0, q1*mu, q2*mu2), FP32 or 16-bit
+    size_t blk_cap = 0;        // bytes
+    float *lo = nullptr;       // compensated-tally remainders
+    size_t lo_cap = 0;
+    double *ff64 = nullptr;    // FP64 tally accumulator
+    size_t ff64_cap = 0;
+    float4 *gblk = nullptr;    // adjoint: cell-block gradients
+    size_t gblk_cap = 0;
+    float *hist = nullptr;     // adjoint: psi entering every segment
+    size_t hist_cap = 0;
+    // batching form
+    float4 *bblk = nullptr;    // cell blocks of all problems of a batch
+    size_t bblk_cap = 0;
+    int *bhist = nullptr, *bperm = nullptr;
+    size_t bhist_cap = 0, bperm_cap = 0;
+    int2 *bqueue = nullptr;
+    size_t bqueue_cap = 0;
+    float *bsave = nullptr;    // autotuner: saved psi and fine_flux
+    size_t bsave_cap = 0;
+    cudaStream_t gstream = nullptr;        // capture stream of the batch graph
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey;       // what the captured graph was built for
+    std::vector<unsigned char> tune_key;   // problem set the tuned choice belongs to
+    int tune_vec = 0, tune_wpb = 0;
     float *table = nullptr;
     int32_t table_n = 0;
     float table_maxval = 0.0f, table_dx = 0.0f, table_lookup = 0.0f;
@@ -61,6 +84,9 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         p->group_stride < p->n_groups || p->n_tracks < 0 || p->n_segments < 0)
         return MOC_ERR_INVALID_ARG;
     if (p->group_stride % 4 != 0) return MOC_ERR_UNSUPPORTED;
+    // cell * group_stride is formed in 32-bit arithmetic by the sweep
+    if ((int64_t)p->n_regions * p->n_intervals * p->group_stride > INT32_MAX)
+        return MOC_ERR_UNSUPPORTED;
     if (!p->track_offsets || !p->sigT || !p->source || !p->fine_flux) return MOC_ERR_INVALID_ARG;
     if (p->n_tracks > 0 && !p->psi) return MOC_ERR_INVALID_ARG;
     if (p->n_segments > 0 && (!p->seg_region || !p->seg_interval || !p->seg_ds))
@@ -71,7 +97,7 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         return MOC_ERR_MISALIGNED;
     if (o->exp_mode != MOC_EXP_FULL && o->exp_mode != MOC_EXP_TABLE) return MOC_ERR_INVALID_ARG;
     if (o->precision != MOC_PREC_FP32 && o->precision != MOC_PREC_BF16 &&
-        o->precision != MOC_PREC_FP16)
+        o->precision != MOC_PREC_FP16 && o->precision != MOC_PREC_FP32_STABLE)
         return MOC_ERR_INVALID_ARG;
     if (o->tally != MOC_TALLY_ATOMIC_FP32 && o->tally != MOC_TALLY_COMPENSATED &&
         o->tally != MOC_TALLY_FP64)
@@ -82,8 +108,10 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
     if (o->vec != 0 && o->vec != 1 && o->vec != 2 && o->vec != 4) return MOC_ERR_INVALID_ARG;
     if (o->warps_per_block < 0 || o->warps_per_block > 8) return MOC_ERR_INVALID_ARG;
     if (!std::isfinite(o->dz) || o->dz == 0.0f) return MOC_ERR_INVALID_ARG;
-    // Forms not built yet in this library version.
-    if (o->precision != MOC_PREC_FP32 || o->tally != MOC_TALLY_ATOMIC_FP32)
+    // The precision forms use the accurate exponential; the table is the plain form's.
+    if (o->exp_mode == MOC_EXP_TABLE && o->precision != MOC_PREC_FP32)
+        return MOC_ERR_UNSUPPORTED;
+    if (o->precision == MOC_PREC_FP32 && o->tally != MOC_TALLY_ATOMIC_FP32)
         return MOC_ERR_UNSUPPORTED;
     return MOC_OK;
 }
@@ -141,10 +169,21 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
                          moc::FwdConfig *c)
 {
     int vec = o->vec;
-    if (vec == 0) vec = p->n_groups > 64 ? 4 : (p->n_groups > 32 ? 2 : 1);
+    if (vec == 0) vec = moc::auto_vec(p->n_groups);
     c->vec = vec;
     c->warps_per_block = o->warps_per_block ? o->warps_per_block : 8;
     c->exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+    c->store = moc::STORE_F32;
+    c->tally = moc::TALLY_F32;
+    if (o->precision != MOC_PREC_FP32) {
+        c->exp_kind = moc::EXPK_STABLE;
+        c->store = o->precision == MOC_PREC_BF16   ? moc::STORE_BF16
+                   : o->precision == MOC_PREC_FP16 ? moc::STORE_F16
+                                                   : moc::STORE_F32;
+        c->tally = o->tally == MOC_TALLY_COMPENSATED ? moc::TALLY_COMP
+                   : o->tally == MOC_TALLY_FP64      ? moc::TALLY_F64
+                                                     : moc::TALLY_F32;
+    }
     const size_t smem = c->exp_kind == moc::EXPK_TABLE ? (size_t)o->table_points * 8 : 0;
     const int per_sm = moc::fwd_blocks_per_sm(*c, smem);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
@@ -157,9 +196,8 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
 {
     moc_status_t s;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
-    const size_t coef_floats = (size_t)ncell * 3 * p->group_stride;
-    if ((s = ensure(h, reinterpret_cast<void **>(&h->coef), &h->coef_cap, coef_floats * 4)))
-        return s;
+    const size_t blk_bytes = (size_t)ncell * p->group_stride * sizeof(float4);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, blk_bytes))) return s;
     if (o->exp_mode == MOC_EXP_TABLE && (s = ensure_table(h, o, st))) return s;
 
     moc::SweepParams sp{};
@@ -173,8 +211,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     sp.reg = p->seg_region;
     sp.itv = p->seg_interval;
     sp.ds = p->seg_ds;
-    sp.sigT = p->sigT;
-    sp.coef = h->coef;
+    sp.blk = h->blk;
     sp.ff = p->fine_flux;
     sp.psi = p->psi;
     sp.weight = o->weight;
@@ -200,20 +237,184 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
 
+    const size_t nff = (size_t)ncell * p->group_stride;
+    if (cfg.tally == moc::TALLY_COMP) {
+        if ((s = ensure(h, reinterpret_cast<void **>(&h->lo), &h->lo_cap, nff * sizeof(float))))
+            return s;
+        sp.lo = h->lo;
+    } else if (cfg.tally == moc::TALLY_F64) {
+        if ((s = ensure(h, reinterpret_cast<void **>(&h->ff64), &h->ff64_cap,
+                        nff * sizeof(double))))
+            return s;
+        sp.ff64 = h->ff64;
+    }
+
     const bool prof = o->profile != 0;
     if (prof && !h->ev[0])
         for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
-    MOC_CUDA(h, moc::launch_prep_coef(p->source, h->coef, p->n_regions, p->n_intervals,
-                                      p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));
+    if (cfg.store == moc::STORE_F32)
+        MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
+                                           p->n_intervals, p->group_stride, o->dz, o->zin,
+                                           o->mu, o->mu2, st));
+    else
+        MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
+                                             p->n_regions, p->n_intervals, p->group_stride,
+                                             o->dz, o->zin, o->mu, o->mu2, st));
+    if (sp.lo) MOC_CUDA(h, cudaMemsetAsync(sp.lo, 0, nff * sizeof(float), st));
+    if (sp.ff64) MOC_CUDA(h, cudaMemsetAsync(sp.ff64, 0, nff * sizeof(double), st));
     MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     MOC_CUDA(h, moc::launch_fwd(sp, cfg, st));
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
+    const bool finish = sp.lo || sp.ff64;
+    if (finish) MOC_CUDA(h, moc::launch_finish(p->fine_flux, sp.lo, sp.ff64, (int64_t)nff, st));
     if (prof) {
-        MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
-        h->timed_launches = 2;
-        h->timed_finish = false;
+        if (finish) MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
+        h->timed_launches = finish ? 3 : 2;
+        h->timed_finish = finish;
     }
+    return MOC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Batching form
+// ------------------------------------------------------------------------------------
+moc_status_t check_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
+                         const moc_fwd_opts_t *o)
+{
+    if (!h || !probs || !o || n < 1 || n > MOC_BATCH_MAX_PROBLEMS) return MOC_ERR_INVALID_ARG;
+    if (o->precision != MOC_PREC_FP32) return MOC_ERR_UNSUPPORTED;  // the plain form
+    for (int32_t k = 0; k < n; k++) {
+        moc_status_t s = check_problem(&probs[k], o);
+        if (s) return s;
+        if (!moc::all_device_accessible(&probs[k])) return MOC_ERR_INVALID_ARG;
+    }
+    return MOC_OK;
+}
+
+void append(std::vector<unsigned char> &key, const void *p, size_t n)
+{
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    key.insert(key.end(), b, b + n);
+}
+
+// The problem set and the options that shape the computation.
+std::vector<unsigned char> set_key(const moc_problem_t *probs, int32_t n, const moc_fwd_opts_t *o)
+{
+    std::vector<unsigned char> key;
+    append(key, probs, sizeof(moc_problem_t) * (size_t)n);
+    const float f[7] = {o->table_max, o->dz, o->zin, o->weight, o->mu, o->mu2, 0.0f};
+    const int32_t i[2] = {(int32_t)o->exp_mode, o->table_points};
+    append(key, f, sizeof(f));
+    append(key, i, sizeof(i));
+    return key;
+}
+
+// Lay out sub-problems, workspace and launch parameters for one (vec, wpb) choice.
+moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
+                         const moc_fwd_opts_t *o, int vec, int wpb, moc::BatchParams &B,
+                         moc::BatchWork &W, int &blocks)
+{
+    moc_status_t s;
+    std::memset(&B, 0, sizeof(B));
+    size_t blk_total = 0, perm_total = 0;
+    for (int32_t k = 0; k < n; k++) {
+        blk_total += (size_t)probs[k].n_regions * probs[k].n_intervals * probs[k].group_stride;
+        perm_total += (size_t)probs[k].n_tracks;
+    }
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->bblk), &h->bblk_cap,
+                    (blk_total ? blk_total : 1) * sizeof(float4))))
+        return s;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->bperm), &h->bperm_cap,
+                    (perm_total ? perm_total : 1) * sizeof(int))))
+        return s;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->bhist), &h->bhist_cap,
+                    sizeof(int) * moc::BATCH_BUCKETS * (MOC_BATCH_MAX_PROBLEMS + 1))))
+        return s;
+    size_t boff = 0;
+    int perm_off = 0, nsub = 0;
+    int64_t items = 0;
+    const int chunk = 32 * vec;
+    for (int32_t k = 0; k < n; k++) {
+        const moc_problem_t &p = probs[k];
+        moc::BatchProb &bp = B.prob[k];
+        bp.off = p.track_offsets;
+        bp.reg = p.seg_region;
+        bp.itv = p.seg_interval;
+        bp.ds = p.seg_ds;
+        bp.blk = h->bblk + boff;
+        bp.ff = p.fine_flux;
+        bp.psi = p.psi;
+        bp.R = p.n_regions;
+        bp.I = p.n_intervals;
+        bp.G = p.n_groups;
+        bp.Gs = p.group_stride;
+        bp.T = p.n_tracks;
+        bp.S = p.n_segments;
+        bp.perm_off = perm_off;
+        boff += (size_t)p.n_regions * p.n_intervals * p.group_stride;
+        perm_off += p.n_tracks;
+        // full chunks of 32*vec groups, then the remainder on narrower sub-warps
+        for (int g = 0; g < p.n_groups; g += chunk) {
+            const int count = p.n_groups - g < chunk ? p.n_groups - g : chunk;
+            const int lanes = (count + vec - 1) / vec;
+            int lpt = 1;
+            while (lpt < lanes) lpt *= 2;
+            if (nsub >= moc::BATCH_MAX_SUB) return MOC_ERR_UNSUPPORTED;
+            moc::BatchSub &sb = B.sub[nsub++];
+            sb.prob = k;
+            sb.g_begin = g;
+            sb.g_count = count;
+            sb.lpt = lpt;
+            sb.item_base = items;
+            const int per_warp = 32 / lpt;
+            items += (p.n_tracks + per_warp - 1) / per_warp;
+        }
+    }
+    B.n_prob = n;
+    B.n_sub = nsub;
+    B.n_items = items;
+    B.weight = o->weight;
+    B.err = h->err;
+    B.counter = h->counter;
+    if (o->exp_mode == MOC_EXP_TABLE) {
+        if ((s = ensure_table(h, o, h->hstream))) return s;
+        B.table = h->table;
+        B.tab_n = h->table_n;
+        B.tab_dx = h->table_dx;
+        B.tab_max = h->table_lookup;
+    }
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->bqueue), &h->bqueue_cap,
+                    (size_t)(items ? items : 1) * sizeof(int2))))
+        return s;
+    W.hist = h->bhist;
+    W.perm = h->bperm;
+    W.queue = h->bqueue;
+    const int ek = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+    const size_t smem = ek == moc::EXPK_TABLE ? (size_t)o->table_points * 8 : 0;
+    const int per_sm = moc::batch_blocks_per_sm(vec, ek, wpb, smem);
+    if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+    blocks = per_sm * h->sm_count;
+    return MOC_OK;
+}
+
+// Enqueue one batched sweep: the coefficient pass of every problem, then the queue and
+// the sweep.
+moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
+                           const moc_fwd_opts_t *o, const moc::BatchParams &B,
+                           const moc::BatchWork &W, int vec, int wpb, int blocks,
+                           cudaStream_t st)
+{
+    for (int32_t k = 0; k < n; k++)
+        MOC_CUDA(h, moc::launch_prep_block(probs[k].sigT, probs[k].source,
+                                           const_cast<float4 *>(B.prob[k].blk),
+                                           probs[k].n_regions, probs[k].n_intervals,
+                                           probs[k].group_stride, o->dz, o->zin, o->mu, o->mu2,
+                                           st));
+    if (B.n_items == 0) return MOC_OK;
+    const int ek = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+    MOC_CUDA(h, moc::launch_batch(B, W, vec, ek, wpb, blocks, st));
     return MOC_OK;
 }
 
@@ -289,7 +490,18 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (!h) return MOC_OK;
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
-    if (h->coef) cudaFree(h->coef);
+    if (h->blk) cudaFree(h->blk);
+    if (h->lo) cudaFree(h->lo);
+    if (h->ff64) cudaFree(h->ff64);
+    if (h->gblk) cudaFree(h->gblk);
+    if (h->hist) cudaFree(h->hist);
+    if (h->bblk) cudaFree(h->bblk);
+    if (h->bhist) cudaFree(h->bhist);
+    if (h->bperm) cudaFree(h->bperm);
+    if (h->bqueue) cudaFree(h->bqueue);
+    if (h->bsave) cudaFree(h->bsave);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->gstream) cudaStreamDestroy(h->gstream);
     if (h->table) cudaFree(h->table);
     if (h->err) cudaFree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
@@ -314,6 +526,257 @@ moc_status_t moc_attenuate_fwd(moc_handle_t h, const moc_problem_t *p,
     for (const void *q : ptrs)
         if (!device_accessible(q)) return MOC_ERR_INVALID_ARG;
     return fwd_device(h, p, o, static_cast<cudaStream_t>(stream));
+}
+
+moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
+                                     const moc_fwd_opts_t *o, void *stream)
+{
+    moc_status_t s = check_batch(h, probs, n, o);
+    if (s) return s;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<unsigned char> key = set_key(probs, n, o);
+    int vec = o->vec, wpb = o->warps_per_block;
+    if (!vec) vec = (h->tune_vec && key == h->tune_key) ? h->tune_vec : 2;
+    if (!wpb) wpb = (h->tune_wpb && key == h->tune_key) ? h->tune_wpb : 8;
+    moc::BatchParams B;
+    moc::BatchWork W;
+    int blocks = 0;
+    if ((s = build_batch(h, probs, n, o, vec, wpb, B, W, blocks))) return s;
+    // the graph is valid for this set, this workspace and this launch shape
+    append(key, &B, sizeof(B));
+    append(key, &W, sizeof(W));
+    const int shape[3] = {vec, wpb, blocks};
+    append(key, shape, sizeof(shape));
+    if (!h->gexec || key != h->gkey) {
+        if (h->gexec) cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+        h->gkey.clear();
+        if (!h->gstream)
+            MOC_CUDA(h, cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+        MOC_CUDA(h, cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeRelaxed));
+        s = enqueue_batch(h, probs, n, o, B, W, vec, wpb, blocks, h->gstream);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
+        if (s) {
+            if (graph) cudaGraphDestroy(graph);
+            return s;
+        }
+        if (e != cudaSuccess) return cuda_fail(h, e, "batch graph capture");
+        const cudaError_t e2 = cudaGraphInstantiate(&h->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e2 != cudaSuccess) {
+            h->gexec = nullptr;
+            return cuda_fail(h, e2, "batch graph instantiate");
+        }
+        h->gkey = key;
+    }
+    const bool prof = o->profile != 0;
+    if (prof && !h->ev[0])
+        for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
+    if (prof) {
+        MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
+        MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
+    }
+    MOC_CUDA(h, cudaGraphLaunch(h->gexec, st));
+    if (prof) {
+        MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
+        h->timed_launches = n + (B.n_items ? 7 : 0);
+        h->timed_finish = false;
+    }
+    return MOC_OK;
+}
+
+moc_status_t moc_autotune_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
+                                const moc_fwd_opts_t *o, void *stream, moc_tune_result_t *res)
+{
+    moc_status_t s = check_batch(h, probs, n, o);
+    if (s) return s;
+    if (!res) return MOC_ERR_INVALID_ARG;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // save psi and fine_flux of every problem; trials run on the real buffers
+    size_t save = 0;
+    for (int32_t k = 0; k < n; k++)
+        save += (size_t)probs[k].group_stride *
+                ((size_t)probs[k].n_tracks + (size_t)probs[k].n_regions * probs[k].n_intervals);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->bsave), &h->bsave_cap,
+                    (save ? save : 1) * sizeof(float))))
+        return s;
+    auto copy_all = [&](bool to_save) -> moc_status_t {
+        size_t at = 0;
+        for (int32_t k = 0; k < n; k++) {
+            const size_t np = (size_t)probs[k].group_stride * probs[k].n_tracks;
+            const size_t nf = (size_t)probs[k].group_stride * probs[k].n_regions *
+                              probs[k].n_intervals;
+            float *sp = h->bsave + at, *sf = h->bsave + at + np;
+            if (np)
+                MOC_CUDA(h, cudaMemcpyAsync(to_save ? sp : probs[k].psi,
+                                            to_save ? probs[k].psi : sp, np * 4,
+                                            cudaMemcpyDeviceToDevice, st));
+            MOC_CUDA(h, cudaMemcpyAsync(to_save ? sf : probs[k].fine_flux,
+                                        to_save ? probs[k].fine_flux : sf, nf * 4,
+                                        cudaMemcpyDeviceToDevice, st));
+            at += np + nf;
+        }
+        return MOC_OK;
+    };
+    if ((s = copy_all(true))) return s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    MOC_CUDA(h, cudaEventCreate(&a));
+    MOC_CUDA(h, cudaEventCreate(&b));
+    std::memset(res, 0, sizeof(*res));
+    res->best_ms = -1.0f;
+    const int vecs[3] = {1, 2, 4}, wpbs[4] = {1, 2, 4, 8};
+    for (int vi = 0; vi < 3 && s == MOC_OK; vi++)
+        for (int wi = 0; wi < 4 && s == MOC_OK; wi++) {
+            moc::BatchParams B;
+            moc::BatchWork W;
+            int blocks = 0;
+            if (build_batch(h, probs, n, o, vecs[vi], wpbs[wi], B, W, blocks)) continue;
+            float best = 1e30f;
+            for (int rep = 0; rep < 3 && s == MOC_OK; rep++) {
+                if ((s = copy_all(false))) break;
+                cudaEventRecord(a, st);
+                s = enqueue_batch(h, probs, n, o, B, W, vecs[vi], wpbs[wi], blocks, st);
+                cudaEventRecord(b, st);
+                if (cudaEventSynchronize(b) != cudaSuccess) s = MOC_ERR_CUDA;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (rep > 0 && ms < best) best = ms;  // the first repeat warms up
+            }
+            const int c = res->n_candidates++;
+            res->candidate_vec[c] = vecs[vi];
+            res->candidate_warps[c] = wpbs[wi];
+            res->candidate_ms[c] = best;
+            if (res->best_ms < 0.0f || best < res->best_ms) {
+                res->best_ms = best;
+                res->vec = vecs[vi];
+                res->warps_per_block = wpbs[wi];
+                res->tracks_per_block = wpbs[wi] * (32 / B.sub[0].lpt);
+            }
+        }
+    const moc_status_t rs = copy_all(false);
+    cudaStreamSynchronize(st);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (s) return s;
+    if (rs) return rs;
+    if (res->n_candidates == 0) return MOC_ERR_UNSUPPORTED;
+    h->tune_key = set_key(probs, n, o);
+    h->tune_vec = res->vec;
+    h->tune_wpb = res->warps_per_block;
+    return MOC_OK;
+}
+
+moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
+                               const float *w, const float *v, float *d_sigT, float *d_source,
+                               float *d_psi_in, void *stream)
+{
+    if (!h || !p || !o) return MOC_ERR_INVALID_ARG;
+    // fine_flux is not used by the adjoint; validate the rest of the problem as the
+    // forward does
+    moc_problem_t q = *p;
+    if (!q.fine_flux) q.fine_flux = const_cast<float *>(p->sigT);
+    moc_fwd_opts_t oo = *o;
+    oo.precision = MOC_PREC_FP32;
+    oo.tally = MOC_TALLY_ATOMIC_FP32;
+    moc_status_t s = check_problem(&q, &oo);
+    if (s) return s;
+    if (o->exp_mode != MOC_EXP_FULL) return MOC_ERR_UNSUPPORTED;
+    if (!w || !d_sigT || !d_source || (p->n_tracks > 0 && (!v || !d_psi_in)))
+        return MOC_ERR_INVALID_ARG;
+    if (!aligned(w, 16) || !aligned(d_sigT, 16) || !aligned(d_source, 16) ||
+        (v && !aligned(v, 16)) || (d_psi_in && !aligned(d_psi_in, 16)))
+        return MOC_ERR_MISALIGNED;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    const void *ptrs[] = {p->track_offsets, p->seg_region, p->seg_interval, p->seg_ds,
+                          p->sigT, p->source, p->psi, w, v, d_sigT, d_source, d_psi_in};
+    for (const void *ptr : ptrs)
+        if (!device_accessible(ptr)) return MOC_ERR_INVALID_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
+    const size_t nff = (size_t)ncell * p->group_stride;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, nff * sizeof(float4))))
+        return s;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->gblk), &h->gblk_cap, nff * sizeof(float4))))
+        return s;
+    const size_t nhist = (size_t)(p->n_segments > 0 ? p->n_segments : 1) * p->group_stride;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->hist), &h->hist_cap, nhist * sizeof(float))))
+        return s;
+
+    moc::AdjParams ap{};
+    moc::SweepParams &sp = ap.fw;
+    sp.R = p->n_regions;
+    sp.I = p->n_intervals;
+    sp.G = p->n_groups;
+    sp.Gs = p->group_stride;
+    sp.T = p->n_tracks;
+    sp.S = p->n_segments;
+    sp.off = p->track_offsets;
+    sp.reg = p->seg_region;
+    sp.itv = p->seg_interval;
+    sp.ds = p->seg_ds;
+    sp.blk = h->blk;
+    sp.psi = p->psi;
+    sp.weight = o->weight;
+    sp.err = h->err;
+    sp.counter = h->counter;
+    const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
+    sp.n_chunks = (p->n_groups + 32 * vec - 1) / (32 * vec);
+    sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
+    ap.hist = h->hist;
+    ap.w = w;
+    ap.v = v;
+    ap.gblk = h->gblk;
+    ap.dpsi_in = d_psi_in;
+
+    // d q_k / d y_{i+m-1} of the axial fit, for the first / interior / last interval
+    // (src/cpu/kernel.c:111-191)
+    float jac[27] = {};
+    {
+        const double dz = o->dz, zin = o->zin, h1 = 1.0 / (2.0 * dz), h2 = 1.0 / (2.0 * dz * dz);
+        const double t0[9] = {0, 1.0 - zin / dz, zin / dz, 0, -1.0 / dz, 1.0 / dz, 0, 0, 0};
+        const double t1[9] = {h1 * zin + h2 * zin * zin, 1.0 - 2.0 * h2 * zin * zin,
+                              -h1 * zin + h2 * zin * zin, h1 + 2.0 * h2 * zin, -4.0 * h2 * zin,
+                              -h1 + 2.0 * h2 * zin, h2, -2.0 * h2, h2};
+        const double t2[9] = {-zin / dz, 1.0 + zin / dz, 0, -1.0 / dz, 1.0 / dz, 0, 0, 0, 0};
+        for (int k = 0; k < 9; k++) {
+            jac[k] = (float)t0[k];
+            jac[9 + k] = (float)t1[k];
+            jac[18 + k] = (float)t2[k];
+        }
+    }
+
+    const bool prof = o->profile != 0;
+    if (prof && !h->ev[0])
+        for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
+    MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
+                                       p->n_intervals, p->group_stride, o->dz, o->zin, o->mu,
+                                       o->mu2, st));
+    MOC_CUDA(h, cudaMemsetAsync(h->gblk, 0, nff * sizeof(float4), st));
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
+    int launches = 1;
+    if (p->n_tracks > 0) {
+        const int bf = moc::adj_blocks_per_sm(vec, false), br = moc::adj_blocks_per_sm(vec, true);
+        if (bf < 1 || br < 1) return MOC_ERR_UNSUPPORTED;
+        MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st));
+        MOC_CUDA(h, moc::launch_adj_forward(ap, vec, bf * h->sm_count, st));
+        MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st));
+        MOC_CUDA(h, moc::launch_adj_reverse(ap, vec, br * h->sm_count, st));
+        launches += 2;
+    }
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
+    MOC_CUDA(h, moc::launch_adj_finish(h->gblk, d_sigT, d_source, p->n_regions, p->n_intervals,
+                                       p->n_groups, p->group_stride, jac, o->mu, o->mu2, st));
+    if (prof) {
+        MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
+        h->timed_launches = launches + 1;
+        h->timed_finish = true;
+    }
+    return MOC_OK;
 }
 
 moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,

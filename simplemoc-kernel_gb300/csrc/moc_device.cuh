@@ -5,6 +5,8 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace moc {
@@ -111,6 +113,61 @@ __device__ __forceinline__ void red_row(float *p, const Vec<VEC> &t, int n_valid
     }
 }
 
+// Compensated tally: hi[g] += t with an atomic that returns the value it added to, then
+// the exact rounding error of that addition (Knuth's TwoSum on the returned value) is
+// reduced into lo[g]. Every addition into hi is an FP32 round-to-nearest addition of the
+// returned value and t, so hi_final + sum(errors) equals hi_start + sum(t) exactly; lo
+// only carries second-order error. hi + lo is combined in FP64 at the end.
+__device__ __forceinline__ float two_sum_err(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+template <int VEC>
+__device__ __forceinline__ void comp_row(float *hi, float *lo, const Vec<VEC> &t, int n_valid)
+{
+    Vec<VEC> old, err;
+    bool done = false;
+    if constexpr (VEC == 4) {
+        if (n_valid >= 4) {
+            asm volatile("atom.global.add.v4.f32 {%0, %1, %2, %3}, [%4], {%5, %6, %7, %8};"
+                         : "=f"(old.v[0]), "=f"(old.v[1]), "=f"(old.v[2]), "=f"(old.v[3])
+                         : "l"(hi), "f"(t.v[0]), "f"(t.v[1]), "f"(t.v[2]), "f"(t.v[3])
+                         : "memory");
+            done = true;
+        }
+    } else if constexpr (VEC == 2) {
+        if (n_valid >= 2) {
+            asm volatile("atom.global.add.v2.f32 {%0, %1}, [%2], {%3, %4};"
+                         : "=f"(old.v[0]), "=f"(old.v[1])
+                         : "l"(hi), "f"(t.v[0]), "f"(t.v[1])
+                         : "memory");
+            done = true;
+        }
+    }
+    if (!done) {
+#pragma unroll
+        for (int k = 0; k < VEC; k++)
+            old.v[k] = k < n_valid ? atomicAdd(hi + k, t.v[k]) : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < VEC; k++) err.v[k] = two_sum_err(old.v[k], t.v[k]);
+    red_row<VEC>(lo, err, n_valid);
+}
+
+// FP64 tally: acc[g] += (double) t, one red.global.add.f64 per group.
+template <int VEC>
+__device__ __forceinline__ void red_row_f64(double *acc, const Vec<VEC> &t, int n_valid)
+{
+#pragma unroll
+    for (int k = 0; k < VEC; k++)
+        if (k < n_valid)
+            asm volatile("red.global.add.f64 [%0], %1;" ::"l"(acc + k), "d"((double)t.v[k])
+                         : "memory");
+}
+
 // ------------------------------------------------------------------------------------
 // Arithmetic helpers.
 // ------------------------------------------------------------------------------------
@@ -148,49 +205,45 @@ __device__ __forceinline__ float exp_neg_rr(float tau)
     return fmaf(p, lo * LN2, p);
 }
 
-// -expm1(-tau) = 1 - exp(-tau) for 0 <= tau < 0.25 by its Taylor series
-// tau - tau^2/2! + tau^3/3! - ... (8 terms; truncation below 2^-24 relative).
-__device__ __forceinline__ float one_minus_exp_series(float tau)
-{
-    float s = 1.0f / 40320.0f;                  // 1/8!
-    s = fmaf(s, -tau, 1.0f / 5040.0f);          // 1/7!
-    s = fmaf(s, -tau, 1.0f / 720.0f);
-    s = fmaf(s, -tau, 1.0f / 120.0f);
-    s = fmaf(s, -tau, 1.0f / 24.0f);
-    s = fmaf(s, -tau, 1.0f / 6.0f);
-    s = fmaf(s, -tau, 0.5f);
-    s = fmaf(s, -tau, 1.0f);
-    return s * tau;
-}
+// The exponential terms of the attenuation, accurate for every tau >= 0:
+//   e = 1 - exp(-tau), p = exp(-tau), tme = tau - e,
+//   cub = tau(tau(tau-3)+6) - 6e.
+// For small tau the direct forms cancel (tme ~ tau^2/2, cub ~ tau^4/4). Below tau = 1
+// all four come from one Taylor sum, s4 = sum_{k>=4} (-1)^k tau^k / k! (Horner in -tau
+// through tau^12; the first omitted term is below 4e-9 of s4 at tau = 1):
+//   cub = 6 s4,  tme = tau^2 (1/2 - tau/6) + s4,  e = tau - tme,  p = 1 - e,
+// none of which cancels there (tme <= tau^2/2, e >= 0.63 tau). From tau = 1 on, p comes
+// from the range-reduced exponential and the cubic cancels at most ~30-fold.
+struct ExpTerms {
+    float e, p, tme, cub;
+};
 
-// tau - (1 - exp(-tau)) = tau^2/2! - tau^3/3! + ... for 0 <= tau < 0.25.
-__device__ __forceinline__ float tau_minus_e_series(float tau)
+__device__ __forceinline__ ExpTerms exp_terms_stable(float tau)
 {
-    float s = 1.0f / 40320.0f;                  // 1/8!
-    s = fmaf(s, -tau, 1.0f / 5040.0f);
-    s = fmaf(s, -tau, 1.0f / 720.0f);
-    s = fmaf(s, -tau, 1.0f / 120.0f);
-    s = fmaf(s, -tau, 1.0f / 24.0f);
-    s = fmaf(s, -tau, 1.0f / 6.0f);
-    s = fmaf(s, -tau, 0.5f);
-    return s * tau * tau;
-}
-
-// tau(tau(tau-3)+6) - 6(1 - exp(-tau)) = 6 (tau^4/4! - tau^5/5! + ...) for
-// 0 <= tau < 0.5 (terms through tau^12).
-__device__ __forceinline__ float cubic_series(float tau)
-{
-    float s = 1.0f / 479001600.0f;              // 1/12!
-    s = fmaf(s, -tau, 1.0f / 39916800.0f);      // 1/11!
-    s = fmaf(s, -tau, 1.0f / 3628800.0f);
-    s = fmaf(s, -tau, 1.0f / 362880.0f);
-    s = fmaf(s, -tau, 1.0f / 40320.0f);
-    s = fmaf(s, -tau, 1.0f / 5040.0f);
-    s = fmaf(s, -tau, 1.0f / 720.0f);
-    s = fmaf(s, -tau, 1.0f / 120.0f);
-    s = fmaf(s, -tau, 1.0f / 24.0f);
-    const float t2 = tau * tau;
-    return 6.0f * s * t2 * t2;
+    ExpTerms r;
+    if (tau < 1.0f) {
+        float h = 1.0f / 479001600.0f;             // 1/12!
+        h = fmaf(h, -tau, 1.0f / 39916800.0f);     // 1/11!
+        h = fmaf(h, -tau, 1.0f / 3628800.0f);
+        h = fmaf(h, -tau, 1.0f / 362880.0f);
+        h = fmaf(h, -tau, 1.0f / 40320.0f);
+        h = fmaf(h, -tau, 1.0f / 5040.0f);
+        h = fmaf(h, -tau, 1.0f / 720.0f);
+        h = fmaf(h, -tau, 1.0f / 120.0f);
+        h = fmaf(h, -tau, 1.0f / 24.0f);
+        const float t2 = tau * tau;
+        const float s4 = h * t2 * t2;
+        r.cub = 6.0f * s4;
+        r.tme = fmaf(t2, fmaf(tau, -1.0f / 6.0f, 0.5f), s4);
+        r.e = tau - r.tme;
+        r.p = 1.0f - r.e;
+    } else {
+        r.p = exp_neg_rr(tau);
+        r.e = 1.0f - r.p;
+        r.tme = tau - r.e;
+        r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
+    }
+    return r;
 }
 
 // The reference's table lookup (src/cpu/kernel.c:337-361), rounded exactly as the

@@ -26,6 +26,20 @@ enum ExpKind : int {
     EXPK_STABLE = 2,  // Taylor branches for small tau, range-reduced ex2 elsewhere
 };
 
+// Storage of the cell blocks (sigT, q0, q1*mu, q2*mu2).
+enum StoreKind : int {
+    STORE_F32 = 0,   // float4 per (cell, group)
+    STORE_BF16 = 1,  // four bf16 per (cell, group), widened to FP32 on load
+    STORE_F16 = 2,   // four fp16 per (cell, group)
+};
+
+// Accumulation of the fine_flux tallies.
+enum TallyKind : int {
+    TALLY_F32 = 0,   // red.global.add.v4.f32 into fine_flux
+    TALLY_COMP = 1,  // atomics into fine_flux + error-free-transform remainders into lo
+    TALLY_F64 = 2,   // red.global.add.f64 into a double accumulator
+};
+
 // Everything a sweep launch reads. Device pointers.
 struct SweepParams {
     int32_t R, I, G, Gs, T, n_chunks;
@@ -34,9 +48,11 @@ struct SweepParams {
     const int32_t *reg;
     const uint8_t *itv;
     const float *ds;
-    const float *sigT;   // [R][Gs]
-    const float *coef;   // [R*I][3][Gs]: q0, q1*mu, q2*mu2
+    const void *blk;     // [R*I][Gs]: (sigT, q0, q1*mu, q2*mu2) per cell and group,
+                         // float4 or four 16-bit values (StoreKind)
     float *ff;           // [R*I][Gs]
+    float *lo;           // [R*I][Gs] compensation remainders (TALLY_COMP)
+    double *ff64;        // [R*I][Gs] double accumulator (TALLY_F64)
     float *psi;          // [T][Gs]
     float weight;
     const float *table;  // [2*tab_n] (slope, intercept) pairs, EXPK_TABLE only
@@ -46,25 +62,106 @@ struct SweepParams {
     unsigned long long *counter;  // work-queue head, zeroed before each launch
 };
 
-// Axial coefficients of every (region, interval): coef[c][0] = q0, [1] = q1*mu,
-// [2] = q2*mu2, rounded exactly as src/cpu/kernel.c:111-191 and the first product of
-// kernel.c:250-251 / 311-322 round them.
-cudaError_t launch_prep_coef(const float *source, float *coef, int R, int I, int Gs,
-                             float dz, float zin, float mu, float mu2, cudaStream_t st);
+// Cell blocks of every (region, interval) and group: blk[c][g] = (sigT of the region,
+// q0, q1*mu, q2*mu2), the coefficients rounded exactly as src/cpu/kernel.c:111-191 and
+// the first product of kernel.c:250-251 / 311-322 round them.
+cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
+                              int I, int Gs, float dz, float zin, float mu, float mu2,
+                              cudaStream_t st);
+// The same blocks rounded to bf16 (store = STORE_BF16) or fp16 (STORE_F16), to nearest.
+cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
+                                int R, int I, int Gs, float dz, float zin, float mu,
+                                float mu2, cudaStream_t st);
+// fine_flux[k] = (float)((double)fine_flux[k] + lo[k]) (or + ff64[k]) over n entries.
+cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_t n,
+                          cudaStream_t st);
 
 // The forward sweep (persistent, one warp per (track, group chunk) work item).
 struct FwdConfig {
     int vec;              // groups per lane: 1, 2, 4
-    int warps_per_block;  // 1..32
+    int warps_per_block;  // 1..8
     int exp_kind;         // ExpKind
     int blocks;           // grid size (0 = fill the GPU)
+    int store = STORE_F32;
+    int tally = TALLY_F32;
 };
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &cfg, cudaStream_t st);
+// Default groups per lane for G groups (measured fastest at G = 64 and 128 on GB300:
+// two groups per lane keeps registers low enough for 32 resident warps per SM).
+inline int auto_vec(int G) { return G > 32 ? 2 : 1; }
 // Resident blocks per SM for a configuration (0 if the configuration is invalid).
 int fwd_blocks_per_sm(const FwdConfig &cfg, size_t smem_bytes);
 
 // Checked mode: scan offsets and segment indices, OR errors into p.err. No writes
 // to psi or fine_flux.
 cudaError_t launch_check(const SweepParams &p, cudaStream_t st);
+
+// ------------------------------------------------------------------------------------
+// Batching form (moc_batch.cu).
+// ------------------------------------------------------------------------------------
+constexpr int BATCH_BUCKETS = 128;   // log-scale track-length buckets, longest first
+constexpr int BATCH_MAX_PROB = 8;
+constexpr int BATCH_MAX_SUB = 16;
+
+struct BatchProb {                   // one problem (device pointers)
+    const int64_t *off;
+    const int32_t *reg;
+    const uint8_t *itv;
+    const float *ds;
+    const float4 *blk;               // its cell blocks (FP32)
+    float *ff;
+    float *psi;
+    int32_t R, I, G, Gs, T, perm_off;  // perm_off: start of its sorted track list
+    int64_t S;
+};
+struct BatchSub {                    // one group range of one problem
+    int32_t prob, g_begin, g_count, lpt;  // lpt: lanes per track (power of two <= 32)
+    int64_t item_base;               // first global item id; items = ceil(T / (32/lpt))
+};
+struct BatchParams {
+    BatchProb prob[BATCH_MAX_PROB];
+    BatchSub sub[BATCH_MAX_SUB];
+    int32_t n_prob, n_sub;
+    int64_t n_items;
+    float weight;
+    const float *table;
+    int32_t tab_n;
+    float tab_dx, tab_max;
+    int32_t *err;
+    unsigned long long *counter;
+};
+struct BatchWork {                   // device workspace of the queue construction
+    int *hist;                       // [(n_prob + 1) * BATCH_BUCKETS]
+    int *perm;                       // [sum T] sorted track ids
+    int2 *queue;                     // [n_items] (sub-problem, first sorted position)
+};
+// Queue construction + the persistent sweep (vec in {1, 2, 4}; ek EXPK_PLAIN/TABLE).
+cudaError_t launch_batch(const BatchParams &B, const BatchWork &W, int vec, int ek,
+                         int warps_per_block, int blocks, cudaStream_t st);
+int batch_blocks_per_sm(int vec, int ek, int warps_per_block, size_t smem);
+
+// ------------------------------------------------------------------------------------
+// Adjoint (moc_adjoint.cu).
+// ------------------------------------------------------------------------------------
+struct AdjParams {
+    SweepParams fw;          // geometry, descriptors, cell blocks (FP32), psi = psi_in,
+                             // weight, err, counter; ff unused
+    float *hist;             // [S][Gs] psi entering each segment (workspace)
+    const float *w;          // [R*I][Gs] dL/dfine_flux
+    const float *v;          // [T][Gs]   dL/dpsi_out
+    float4 *gblk;            // [R*I][Gs] (dL/dsigT, dL/da0, dL/da1, dL/da2) per cell
+    float *dpsi_in;          // [T][Gs]   dL/dpsi_in (out)
+};
+// Forward pass that records psi entering every segment, then the reverse sweep that
+// scatters the cell-block gradients; vec in {1, 2, 4}.
+cudaError_t launch_adj_forward(const AdjParams &p, int vec, int blocks, cudaStream_t st);
+cudaError_t launch_adj_reverse(const AdjParams &p, int vec, int blocks, cudaStream_t st);
+int adj_blocks_per_sm(int vec, bool reverse);
+// dL/dsigT[r][g] = sum over intervals of the sigT gradients; dL/dsource through the
+// transpose of the axial fit (jac[type][k][m]: d q_k / d y_{i+m-1}, type 0 = first
+// interval, 1 = interior, 2 = last), q1 = a1 / mu and q2 = a2 / mu2.
+cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,
+                              int G, int Gs, const float *jac27, float mu, float mu2,
+                              cudaStream_t st);
 
 }  // namespace moc

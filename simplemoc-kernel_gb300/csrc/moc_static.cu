@@ -5,9 +5,9 @@
 // afford the device-wide synchronisation cudaMalloc/cudaFree may cause while other
 // streams run, or a stateless call site with nowhere to keep a handle. For them this
 // entry point sweeps with the same kernels as moc_attenuate_fwd, but its scratch (the
-// axial coefficients, the exponential table, the work-queue head and the error word)
-// lives in one file-scope __device__ array of fixed size, which every GPU that loads
-// the library holds until the process exits.
+// per-cell blocks of sigT and axial coefficients, the exponential table, the work-queue
+// head and the error word) lives in one file-scope __device__ array of fixed size,
+// which every GPU that loads the library holds until the process exits.
 //
 // That array's name, used in host code, is only a host-side stand-in for the symbol,
 // not a device address: a kernel given it would fault or, where the GPU can reach host
@@ -18,7 +18,7 @@
 // the rest, so make the first call on each device before any stream capture.
 //
 // Every call shares the one array and it keeps the last call's contents: each call
-// clears the work-queue head and error word before its kernels run and rewrites the
+// clears the work-queue head and error word before its kernels run and rewrites the cell
 // coefficients (and the table in table mode). Calls whose kernels overlap on the GPU —
 // on different streams, or from different host threads — race on the array and give
 // wrong results; order them on one stream.
@@ -32,11 +32,12 @@ namespace {
 // Layout of the scratch array (bytes):
 //   [0, 256)                    work-queue head (u64 at 0) and error word (i32 at 8)
 //   [256, 256 + TABLE_BYTES)    exponential table, MOC_NOALLOC_MAX_TABLE_POINTS pairs
-//   [COEF_OFF, end)             axial coefficients, MOC_NOALLOC_MAX_COEF_FLOATS floats
+//   [BLK_OFF, end)              cell blocks (sigT, q0, q1*mu, q2*mu2), 16 bytes for each
+//                               of MOC_NOALLOC_MAX_CELL_GROUPS (region, interval, group)
 constexpr size_t CTRL_BYTES = 256;
 constexpr size_t TABLE_BYTES = ((size_t)MOC_NOALLOC_MAX_TABLE_POINTS * 8 + 255) / 256 * 256;
-constexpr size_t COEF_OFF = CTRL_BYTES + TABLE_BYTES;
-constexpr size_t SCRATCH_BYTES = COEF_OFF + (size_t)MOC_NOALLOC_MAX_COEF_FLOATS * 4;
+constexpr size_t BLK_OFF = CTRL_BYTES + TABLE_BYTES;
+constexpr size_t SCRATCH_BYTES = BLK_OFF + (size_t)MOC_NOALLOC_MAX_CELL_GROUPS * 16;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
@@ -85,8 +86,9 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
 {
     moc_status_t s = moc::check_args(p, o);
     if (s) return s;
-    const int64_t coef_floats = (int64_t)p->n_regions * p->n_intervals * 3 * p->group_stride;
-    if (coef_floats > MOC_NOALLOC_MAX_COEF_FLOATS) return MOC_ERR_TOO_LARGE;
+    if (o->precision != MOC_PREC_FP32) return MOC_ERR_UNSUPPORTED;  // the plain form only
+    const int64_t cell_groups = (int64_t)p->n_regions * p->n_intervals * p->group_stride;
+    if (cell_groups > MOC_NOALLOC_MAX_CELL_GROUPS) return MOC_ERR_TOO_LARGE;
     if (o->exp_mode == MOC_EXP_TABLE && o->table_points > MOC_NOALLOC_MAX_TABLE_POINTS)
         return MOC_ERR_TOO_LARGE;
     if (!moc::all_device_accessible(p)) return MOC_ERR_INVALID_ARG;
@@ -101,7 +103,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     auto *counter = reinterpret_cast<unsigned long long *>(base);
     auto *err = reinterpret_cast<int32_t *>(base + 8);
     auto *table = reinterpret_cast<float *>(base + CTRL_BYTES);
-    auto *coef = reinterpret_cast<float *>(base + COEF_OFF);
+    auto *blk = reinterpret_cast<float4 *>(base + BLK_OFF);
 
     moc::SweepParams sp{};
     sp.R = p->n_regions;
@@ -114,8 +116,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     sp.reg = p->seg_region;
     sp.itv = p->seg_interval;
     sp.ds = p->seg_ds;
-    sp.sigT = p->sigT;
-    sp.coef = coef;
+    sp.blk = blk;
     sp.ff = p->fine_flux;
     sp.psi = p->psi;
     sp.weight = o->weight;
@@ -143,7 +144,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     if (p->n_tracks == 0) return MOC_OK;
 
     moc::FwdConfig cfg;
-    cfg.vec = o->vec ? o->vec : (p->n_groups > 64 ? 4 : (p->n_groups > 32 ? 2 : 1));
+    cfg.vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
     cfg.warps_per_block = o->warps_per_block ? o->warps_per_block : 8;
     cfg.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
     const size_t smem = cfg.exp_kind == moc::EXPK_TABLE ? (size_t)o->table_points * 8 : 0;
@@ -153,8 +154,8 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
 
-    NA_CUDA(moc::launch_prep_coef(p->source, coef, p->n_regions, p->n_intervals,
-                                  p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));
+    NA_CUDA(moc::launch_prep_block(p->sigT, p->source, blk, p->n_regions, p->n_intervals,
+                                   p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));
     NA_CUDA(moc::launch_fwd(sp, cfg, st));
     return MOC_OK;
 }

@@ -7,12 +7,18 @@
 // independent, so a track's chunks are independent items. Warps take items from a
 // global queue head (one atomicAdd per item), so tracks of uneven length balance.
 //
-// Per segment a warp reads: the segment descriptor (region, interval, ds; one coalesced
-// load per 32 segments, broadcast by shuffles and fetched one window ahead), the sigT
-// row of the region and the 2 or 3 axial-coefficient rows of the cell (128-bit loads),
-// and adds the tally row into fine_flux with vector reductions. The rows of the next
-// segment are loaded before the current one is computed, so their L2 latency overlaps
-// the arithmetic.
+// The sweep is bound by instruction issue, so everything that is not arithmetic is cut
+// down:
+//  * a prep pass writes one block per (region, interval) cell, interleaved by group:
+//    blk[cell][g] = (sigT, q0, q1*mu, q2*mu2), so a segment needs one address and a lane
+//    reads its VEC groups' four values with VEC 128-bit loads at immediate offsets;
+//    q2*mu2 is 0 at the first and last interval, so no branch on the interval;
+//  * segment descriptors are decoded lane-parallel: lane l validates segment wb+l of a
+//    32-segment window and forms its cell index once; the warp then only shuffles
+//    (cell, ds) per segment; the next window is loaded 32 segments ahead;
+//  * the segment loop is unrolled by two with ping-pong registers: the block of segment
+//    j+1 is loaded before segment j is computed, without register moves.
+// Tallies go out as red.global.add.v4.f32 (one L2 request per lane, 16 bytes).
 #include "moc_device.cuh"
 #include "moc_internal.h"
 
@@ -24,45 +30,71 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // ------------------------------------------------------------------------------------
 // Axial fit, src/cpu/kernel.c:111-191, rounded as the reference's C rounds it (no
-// contraction), then the first product of q1 * mu * ... and q2 * mu2 * ....
+// contraction), then the first product of q1 * mu * ... and q2 * mu2 * ...
+// (kernel.c:250-251, 311-322), packed with the region's sigT into the cell block.
 // ------------------------------------------------------------------------------------
-__global__ void prep_coef_kernel(const float *__restrict__ source, float *__restrict__ coef,
-                                 int R, int I, int Gs, float dz, float zin, float mu, float mu2)
+__device__ __forceinline__ float4 cell_block(const float *__restrict__ sigT,
+                                             const float *__restrict__ source, int64_t k, int I,
+                                             int Gs, float dz, float zin, float mu, float mu2)
+{
+    const int64_t cell = k / Gs;
+    const int g = (int)(k - cell * Gs);
+    const int64_t r = cell / I;
+    const int i = (int)(cell - r * I);
+    const float *row = source + cell * Gs + g;
+    float q0, q1, q2;
+    if (i == 0) {
+        const float y2 = row[0], y3 = row[Gs];
+        const float c1 = __fdiv_rn(__fsub_rn(y3, y2), dz);
+        q0 = __fadd_rn(y2, __fmul_rn(c1, zin));
+        q1 = c1;
+        q2 = 0.0f;
+    } else if (i == I - 1) {
+        const float y1 = row[-Gs], y2 = row[0];
+        const float c1 = __fdiv_rn(__fsub_rn(y2, y1), dz);
+        q0 = __fadd_rn(y2, __fmul_rn(c1, zin));
+        q1 = c1;
+        q2 = 0.0f;
+    } else {
+        const float y1 = row[-Gs], y2 = row[0], y3 = row[Gs];
+        const float c1 = __fdiv_rn(__fsub_rn(y1, y3), __fmul_rn(2.0f, dz));
+        const float c2 = __fdiv_rn(__fadd_rn(__fsub_rn(y1, __fmul_rn(2.0f, y2)), y3),
+                                   __fmul_rn(__fmul_rn(2.0f, dz), dz));
+        q0 = __fadd_rn(__fadd_rn(y2, __fmul_rn(c1, zin)), __fmul_rn(__fmul_rn(c2, zin), zin));
+        q1 = __fadd_rn(c1, __fmul_rn(__fmul_rn(2.0f, c2), zin));
+        q2 = c2;
+    }
+    return make_float4(sigT[r * Gs + g], q0, __fmul_rn(q1, mu), __fmul_rn(q2, mu2));
+}
+
+// ST = STORE_F32 writes float4 blocks; STORE_BF16 / STORE_F16 round them to 16 bits (to
+// nearest even) and write four 16-bit values per (cell, group).
+template <int ST>
+__global__ void prep_block_kernel(const float *__restrict__ sigT,
+                                  const float *__restrict__ source, void *__restrict__ blk,
+                                  int R, int I, int Gs, float dz, float zin, float mu, float mu2)
 {
     const int64_t n = (int64_t)R * I * Gs;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t cell = k / Gs;
-        const int g = (int)(k - cell * Gs);
-        const int i = (int)(cell % I);
-        const float *row = source + cell * Gs + g;
-        float q0, q1, q2;
-        if (i == 0) {
-            const float y2 = row[0], y3 = row[Gs];
-            const float c1 = __fdiv_rn(__fsub_rn(y3, y2), dz);
-            q0 = __fadd_rn(y2, __fmul_rn(c1, zin));
-            q1 = c1;
-            q2 = 0.0f;
-        } else if (i == I - 1) {
-            const float y1 = row[-Gs], y2 = row[0];
-            const float c1 = __fdiv_rn(__fsub_rn(y2, y1), dz);
-            q0 = __fadd_rn(y2, __fmul_rn(c1, zin));
-            q1 = c1;
-            q2 = 0.0f;
+        const float4 v = cell_block(sigT, source, k, I, Gs, dz, zin, mu, mu2);
+        if constexpr (ST == STORE_F32) {
+            static_cast<float4 *>(blk)[k] = v;
         } else {
-            const float y1 = row[-Gs], y2 = row[0], y3 = row[Gs];
-            const float c1 = __fdiv_rn(__fsub_rn(y1, y3), __fmul_rn(2.0f, dz));
-            const float c2 = __fdiv_rn(__fadd_rn(__fsub_rn(y1, __fmul_rn(2.0f, y2)), y3),
-                                       __fmul_rn(__fmul_rn(2.0f, dz), dz));
-            q0 = __fadd_rn(__fadd_rn(y2, __fmul_rn(c1, zin)),
-                           __fmul_rn(__fmul_rn(c2, zin), zin));
-            q1 = __fadd_rn(c1, __fmul_rn(__fmul_rn(2.0f, c2), zin));
-            q2 = c2;
+            uint32_t w0, w1;
+            if constexpr (ST == STORE_BF16) {
+                const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
+                const __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
+                w0 = *reinterpret_cast<const uint32_t *>(&a);
+                w1 = *reinterpret_cast<const uint32_t *>(&b);
+            } else {
+                const __half2 a = __floats2half2_rn(v.x, v.y);
+                const __half2 b = __floats2half2_rn(v.z, v.w);
+                w0 = *reinterpret_cast<const uint32_t *>(&a);
+                w1 = *reinterpret_cast<const uint32_t *>(&b);
+            }
+            static_cast<uint2 *>(blk)[k] = make_uint2(w0, w1);
         }
-        float *out = coef + cell * 3 * Gs + g;
-        out[0] = q0;
-        out[Gs] = __fmul_rn(q1, mu);
-        out[2 * Gs] = __fmul_rn(q2, mu2);
     }
 }
 
@@ -70,9 +102,48 @@ __global__ void prep_coef_kernel(const float *__restrict__ source, float *__rest
 // The per-(segment, group) arithmetic.
 // ------------------------------------------------------------------------------------
 template <int VEC>
-struct Rows {
-    Vec<VEC> s, a0, a1, a2;
+struct Blk {
+    float4 v[VEC];  // per group: (sigT, q0, q1*mu, q2*mu2)
 };
+
+// Block of VEC groups at element index idx (= cell * Gs + g0). FP32 blocks are 16 bytes
+// per group; BF16/FP16 blocks 8 bytes (four 16-bit values), widened to FP32 on load.
+template <int VEC, int ST>
+__device__ __forceinline__ void load_blk(const void *base, int idx, Blk<VEC> &b)
+{
+    if constexpr (ST == STORE_F32) {
+        const float4 *p = static_cast<const float4 *>(base) + idx;
+#pragma unroll
+        for (int k = 0; k < VEC; k++) b.v[k] = __ldg(p + k);
+    } else {
+        const uint2 *p = static_cast<const uint2 *>(base) + idx;
+        uint2 w[VEC];
+        if constexpr (VEC == 4) {
+            const uint4 a = __ldg(reinterpret_cast<const uint4 *>(p));
+            const uint4 c = __ldg(reinterpret_cast<const uint4 *>(p) + 1);
+            w[0] = make_uint2(a.x, a.y); w[1] = make_uint2(a.z, a.w);
+            w[2] = make_uint2(c.x, c.y); w[3] = make_uint2(c.z, c.w);
+        } else if constexpr (VEC == 2) {
+            const uint4 a = __ldg(reinterpret_cast<const uint4 *>(p));
+            w[0] = make_uint2(a.x, a.y); w[1] = make_uint2(a.z, a.w);
+        } else {
+            w[0] = __ldg(p);
+        }
+#pragma unroll
+        for (int k = 0; k < VEC; k++) {
+            if constexpr (ST == STORE_BF16) {
+                b.v[k] = make_float4(__uint_as_float(w[k].x << 16),
+                                     __uint_as_float(w[k].x & 0xffff0000u),
+                                     __uint_as_float(w[k].y << 16),
+                                     __uint_as_float(w[k].y & 0xffff0000u));
+            } else {
+                const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&w[k].x));
+                const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&w[k].y));
+                b.v[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
+            }
+        }
+    }
+}
 
 struct TableRef {
     const float2 *tab;
@@ -80,16 +151,16 @@ struct TableRef {
     float dx, max;
 };
 
-// src/cpu/kernel.c:200-332 for VEC groups. a1 = q1*mu and a2 = q2*mu2 come from the
-// prep pass. Divisions by sigT powers become products with one reciprocal.
+// src/cpu/kernel.c:200-332 for VEC groups. Divisions by sigT powers become products with
+// one reciprocal.
 template <int VEC, int EK>
-__device__ __forceinline__ void attenuate(const Rows<VEC> &x, float ds, float weight,
+__device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float weight,
                                           const TableRef &tr, Vec<VEC> &psi,
                                           Vec<VEC> &tally)
 {
 #pragma unroll
     for (int k = 0; k < VEC; k++) {
-        const float s = x.s.v[k], a0 = x.a0.v[k], a1 = x.a1.v[k], a2 = x.a2.v[k];
+        const float s = x.v[k].x, a0 = x.v[k].y, a1 = x.v[k].z, a2 = x.v[k].w;
         const float ps = psi.v[k];
         const float tau = __fmul_rn(s, ds);  // kept exact: the table index depends on it
         float e, p, tme, cub;
@@ -104,16 +175,11 @@ __device__ __forceinline__ void attenuate(const Rows<VEC> &x, float ds, float we
             tme = tau - e;
             cub = tau * (tau * (tau - 3.0f) + 6.0f) - 6.0f * e;
         } else {
-            if (tau < 0.25f) {
-                e = one_minus_exp_series(tau);
-                tme = tau_minus_e_series(tau);
-                p = 1.0f - e;
-            } else {
-                p = exp_neg_rr(tau);
-                e = 1.0f - p;
-                tme = tau - e;
-            }
-            cub = tau < 1.0f ? cubic_series(tau) : tau * (tau * (tau - 3.0f)) + 6.0f * tme;
+            const ExpTerms x = exp_terms_stable(tau);
+            e = x.e;
+            p = x.p;
+            tme = x.tme;
+            cub = x.cub;
         }
         const float rs = rcp_approx(s);
         const float rs2 = rs * rs;
@@ -135,37 +201,25 @@ __device__ __forceinline__ void attenuate(const Rows<VEC> &x, float ds, float we
     }
 }
 
-template <int VEC>
-__device__ __forceinline__ void load_rows(const SweepParams &P, int r, int iv, int g0,
-                                          Rows<VEC> &x)
+// Lane-parallel descriptor decode of segment j: its cell index (or -1 if the region or
+// interval is out of range, reported once through the error word) and its ds.
+__device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t end, int &cell,
+                                       float &ds)
 {
-    x.s = ld_row<VEC>(P.sigT + (int64_t)r * P.Gs + g0);
-    const float *c = P.coef + ((int64_t)r * P.I + iv) * 3 * P.Gs + g0;
-    x.a0 = ld_row<VEC>(c);
-    x.a1 = ld_row<VEC>(c + P.Gs);
-    if (iv > 0 && iv < P.I - 1) {
-        x.a2 = ld_row<VEC>(c + 2 * P.Gs);
-    } else {
-#pragma unroll
-        for (int k = 0; k < VEC; k++) x.a2.v[k] = 0.0f;
-    }
-}
-
-__device__ __forceinline__ void load_desc(const SweepParams &P, int64_t j, int64_t end,
-                                          int &r, int &iv, float &d)
-{
+    cell = -1;
+    ds = 0.0f;
     if (j < end) {
-        r = ld_stream(P.reg + j);
-        iv = ld_stream(P.itv + j);
-        d = ld_stream(P.ds + j);
-    } else {
-        r = 0;
-        iv = 0;
-        d = 0.0f;
+        const int r = ld_stream(P.reg + j);
+        const int iv = ld_stream(P.itv + j);
+        ds = ld_stream(P.ds + j);
+        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I)
+            cell = r * P.I + iv;
+        else
+            atomicOr(P.err, DEVERR_INDEX);
     }
 }
 
-template <int VEC, int EK>
+template <int VEC, int EK, int ST, int TL>
 __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int lane,
                                            const TableRef &tr)
 {
@@ -179,62 +233,68 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
         return;
     }
-    float *psi_row = P.psi + (int64_t)t * P.Gs + g0;
+    const int Gs = P.Gs;
+    float *psi_row = P.psi + (int64_t)t * Gs + g0;
     Vec<VEC> psi;
     if (act) psi = ld_psi<VEC>(psi_row, nvalid);
 
     // Descriptor windows: A = segments [wb, wb+32), B = the next 32.
     int64_t wb = beg;
-    int rA, iA, rB, iB;
+    int cA, cB;
     float dA, dB;
-    load_desc(P, wb + lane, end, rA, iA, dA);
-    load_desc(P, wb + 32 + lane, end, rB, iB, dB);
-
-    Rows<VEC> cur;
-    int rc = __shfl_sync(FULL, rA, 0), ic = __shfl_sync(FULL, iA, 0);
-    float dc = __shfl_sync(FULL, dA, 0);
-    bool okc = (unsigned)rc < (unsigned)P.R && (unsigned)ic < (unsigned)P.I;
-    if (beg < end && okc && act) load_rows<VEC>(P, rc, ic, g0, cur);
-
-    for (int64_t j = beg; j < end; ++j) {
-        Rows<VEC> nxt;
-        int rn = 0, in_ = 0;
-        float dn = 0.0f;
-        bool okn = false;
-        const int64_t jn = j + 1;
-        if (jn < end) {
-            int k = (int)(jn - wb);
-            if (k == 32) {
-                rA = rB; iA = iB; dA = dB;
-                wb += 32;
-                k = 0;
-                load_desc(P, wb + 32 + lane, end, rB, iB, dB);
-            }
-            rn = __shfl_sync(FULL, rA, k);
-            in_ = __shfl_sync(FULL, iA, k);
-            dn = __shfl_sync(FULL, dA, k);
-            okn = (unsigned)rn < (unsigned)P.R && (unsigned)in_ < (unsigned)P.I;
-            if (okn && act) load_rows<VEC>(P, rn, in_, g0, nxt);
+    decode(P, wb + lane, end, cA, dA);
+    decode(P, wb + 32 + lane, end, cB, dB);
+    auto desc = [&](int64_t j, int &c, float &d) {
+        int k = (int)(j - wb);
+        if (k >= 32) {
+            cA = cB;
+            dA = dB;
+            wb += 32;
+            k -= 32;
+            decode(P, wb + 32 + lane, end, cB, dB);
         }
-        if (okc) {
-            if (act) {
-                Vec<VEC> tally;
-                attenuate<VEC, EK>(cur, dc, P.weight, tr, psi, tally);
-                red_row<VEC>(P.ff + ((int64_t)rc * P.I + ic) * P.Gs + g0, tally, nvalid);
-            }
-        } else if (lane == 0) {
-            atomicOr(P.err, DEVERR_INDEX);
+        c = __shfl_sync(FULL, cA, k);
+        d = __shfl_sync(FULL, dA, k);
+    };
+    auto step = [&](const Blk<VEC> &b, int c, float d) {
+        if (c >= 0 && act) {
+            Vec<VEC> tally;
+            attenuate<VEC, EK>(b, d, P.weight, tr, psi, tally);
+            const int idx = c * Gs + g0;
+            if constexpr (TL == TALLY_F32)
+                red_row<VEC>(P.ff + idx, tally, nvalid);
+            else if constexpr (TL == TALLY_COMP)
+                comp_row<VEC>(P.ff + idx, P.lo + idx, tally, nvalid);
+            else
+                red_row_f64<VEC>(P.ff64 + idx, tally, nvalid);
         }
-        cur = nxt;
-        rc = rn;
-        ic = in_;
-        dc = dn;
-        okc = okn;
+    };
+
+    Blk<VEC> b0, b1;
+    int c0 = -1, c1 = -1;
+    float d0 = 0.0f, d1 = 0.0f;
+    if (beg < end) {
+        desc(beg, c0, d0);
+        if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+    }
+    for (int64_t j = beg; j < end; j += 2) {
+        const bool has1 = j + 1 < end;
+        if (has1) {
+            desc(j + 1, c1, d1);
+            if (c1 >= 0 && act) load_blk<VEC, ST>(P.blk, c1 * Gs + g0, b1);
+        }
+        step(b0, c0, d0);
+        if (!has1) break;
+        if (j + 2 < end) {
+            desc(j + 2, c0, d0);
+            if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+        }
+        step(b1, c1, d1);
     }
     if (act) st_psi<VEC>(psi_row, psi, nvalid);
 }
 
-template <int VEC, int EK>
+template <int VEC, int EK, int ST, int TL>
 __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
 {
     extern __shared__ float2 s_tab[];
@@ -251,7 +311,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)P.n_items) break;
-        sweep_item<VEC, EK>(P, (int64_t)item, lane, tr);
+        sweep_item<VEC, EK, ST, TL>(P, (int64_t)item, lane, tr);
     }
 }
 
@@ -273,37 +333,105 @@ __global__ void check_kernel(const SweepParams P)
     if (bad) atomicOr(P.err, bad);
 }
 
-template <int VEC, int EK>
+__global__ void finish_kernel(float *__restrict__ ff, const float *__restrict__ lo,
+                              const double *__restrict__ ff64, int64_t n)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const double add = lo ? (double)lo[k] : ff64[k];
+        ff[k] = (float)((double)ff[k] + add);
+    }
+}
+
+template <int VEC, int EK, int ST, int TL>
 const void *fwd_fn()
 {
-    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK>);
+    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL>);
+}
+
+// The instantiated (exp, storage, tally) combinations, for every VEC:
+//   plain FP32 / table FP32 with FP32 atomics (the drop-in),
+//   stable math with FP32 storage and all three tally kinds,
+//   stable math with BF16 / FP16 storage and all three tally kinds.
+template <int V>
+const void *pick_vec(const FwdConfig &c)
+{
+    if (c.store == STORE_F32) {
+        if (c.exp_kind == EXPK_PLAIN && c.tally == TALLY_F32)
+            return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>();
+        if (c.exp_kind == EXPK_TABLE && c.tally == TALLY_F32)
+            return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>();
+        if (c.exp_kind == EXPK_STABLE) {
+            if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>();
+            if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>();
+            if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>();
+        }
+        return nullptr;
+    }
+    if (c.exp_kind != EXPK_STABLE) return nullptr;
+    if (c.store == STORE_BF16) {
+        if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>();
+        if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>();
+        if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F64>();
+    }
+    if (c.store == STORE_F16) {
+        if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32>();
+        if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_COMP>();
+        if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F64>();
+    }
+    return nullptr;
 }
 
 const void *pick(const FwdConfig &c)
 {
-#define MOC_PICK(V)                                                 \
-    if (c.vec == V) {                                               \
-        if (c.exp_kind == EXPK_PLAIN) return fwd_fn<V, EXPK_PLAIN>();   \
-        if (c.exp_kind == EXPK_TABLE) return fwd_fn<V, EXPK_TABLE>();   \
-        if (c.exp_kind == EXPK_STABLE) return fwd_fn<V, EXPK_STABLE>(); \
-    }
-    MOC_PICK(1)
-    MOC_PICK(2)
-    MOC_PICK(4)
-#undef MOC_PICK
+    if (c.vec == 1) return pick_vec<1>(c);
+    if (c.vec == 2) return pick_vec<2>(c);
+    if (c.vec == 4) return pick_vec<4>(c);
     return nullptr;
 }
 
 }  // namespace
 
-cudaError_t launch_prep_coef(const float *source, float *coef, int R, int I, int Gs,
-                             float dz, float zin, float mu, float mu2, cudaStream_t st)
+static int grid_for(int64_t n)
+{
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    return (int)(blocks < 1 ? 1 : blocks);
+}
+
+cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
+                              int I, int Gs, float dz, float zin, float mu, float mu2,
+                              cudaStream_t st)
 {
     const int64_t n = (int64_t)R * I * Gs;
     if (n == 0) return cudaSuccess;
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    prep_coef_kernel<<<blocks, 256, 0, st>>>(source, coef, R, I, Gs, dz, zin, mu, mu2);
+    prep_block_kernel<STORE_F32><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs, dz,
+                                                               zin, mu, mu2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
+                                int R, int I, int Gs, float dz, float zin, float mu,
+                                float mu2, cudaStream_t st)
+{
+    const int64_t n = (int64_t)R * I * Gs;
+    if (n == 0) return cudaSuccess;
+    if (store == STORE_BF16)
+        prep_block_kernel<STORE_BF16><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
+                                                                    dz, zin, mu, mu2);
+    else if (store == STORE_F16)
+        prep_block_kernel<STORE_F16><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
+                                                                   dz, zin, mu, mu2);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_t n,
+                          cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    finish_kernel<<<grid_for(n), 256, 0, st>>>(ff, lo, ff64, n);
     return cudaGetLastError();
 }
 

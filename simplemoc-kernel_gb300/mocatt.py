@@ -40,6 +40,7 @@ MOC_EXP_TABLE = 1
 MOC_PREC_FP32 = 0
 MOC_PREC_BF16 = 1
 MOC_PREC_FP16 = 2
+MOC_PREC_FP32_STABLE = 3
 MOC_TALLY_ATOMIC_FP32 = 0
 MOC_TALLY_COMPENSATED = 1
 MOC_TALLY_FP64 = 2
@@ -73,6 +74,13 @@ class MocTimings(C.Structure):
                 ("launches", C.c_int32)]
 
 
+class MocTuneResult(C.Structure):
+    _fields_ = [("vec", C.c_int32), ("warps_per_block", C.c_int32),
+                ("tracks_per_block", C.c_int32), ("best_ms", C.c_float),
+                ("n_candidates", C.c_int32), ("candidate_vec", C.c_int32 * 16),
+                ("candidate_warps", C.c_int32 * 16), ("candidate_ms", C.c_float * 16)]
+
+
 class SynthSpec(C.Structure):
     _fields_ = [
         ("seed", C.c_uint64), ("n_regions", C.c_int32), ("n_intervals", C.c_int32),
@@ -97,6 +105,12 @@ ABI = {
                                       C.POINTER(C.c_float)]),
     "moc_last_timings": (C.c_int, [_P, C.POINTER(MocTimings)]),
     "moc_attenuate_fwd_noalloc": (C.c_int, [C.POINTER(MocProblem), C.POINTER(MocFwdOpts), _P]),
+    "moc_attenuate_adj": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts), _P, _P,
+                                    _P, _P, _P, _P]),
+    "moc_attenuate_fwd_batch": (C.c_int, [_P, C.POINTER(MocProblem), C.c_int32,
+                                          C.POINTER(MocFwdOpts), _P]),
+    "moc_autotune_batch": (C.c_int, [_P, C.POINTER(MocProblem), C.c_int32,
+                                     C.POINTER(MocFwdOpts), _P, C.POINTER(MocTuneResult)]),
     "moc_status_string": (C.c_char_p, [C.c_int]),
     "moc_last_error": (C.c_char_p, [_P]),
     "moc_abi_version": (C.c_int32, []),
@@ -385,6 +399,24 @@ class Handle:
         prob = dp.c_struct()
         self.check(lib().moc_attenuate_fwd(self._h, C.byref(prob), C.byref(opts),
                                            C.c_void_p(s.cuda_stream)))
+
+    def adj(self, dp: DeviceProblem, w, v, opts: MocFwdOpts | None = None, stream=None):
+        """moc_attenuate_adj: gradients of L = sum w . fine_flux_out + sum v . psi_out with
+        respect to sigT, source and the incoming psi (dp.psi, which is not modified).
+        w, v: device float32 tensors shaped like fine_flux and psi. Returns torch tensors
+        (d_sigT, d_source, d_psi_in)."""
+        import torch
+        opts = opts or default_opts()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        d_sig = torch.zeros_like(dp.sigT)
+        d_src = torch.zeros_like(dp.source)
+        d_psi = torch.zeros_like(dp.psi)
+        prob = dp.c_struct()
+        self.check(lib().moc_attenuate_adj(self._h, C.byref(prob), C.byref(opts),
+                                           w.data_ptr(), v.data_ptr(), d_sig.data_ptr(),
+                                           d_src.data_ptr(), d_psi.data_ptr(),
+                                           C.c_void_p(s.cuda_stream)))
+        return d_sig, d_src, d_psi
 
     def fwd_host(self, hp: HostProblem, opts: MocFwdOpts | None = None):
         opts = opts or default_opts()

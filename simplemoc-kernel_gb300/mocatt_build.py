@@ -29,7 +29,8 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
     "-I" + INCLUDE, "-I" + CSRC,
 ]
-CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu"]
+CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu", "moc_adjoint.cu",
+              "moc_batch.cu"]
 
 LIB = os.path.join(BUILD, "libmocatt.so")
 SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")

@@ -1,0 +1,153 @@
+"""The adjoint sweep (moc_attenuate_adj) against the FP64 CPU adjoint, FP64 central
+differences, and torch.autograd.gradcheck through a test-only autograd Function.
+
+Workload: 5,000 tracks with lognormal lengths (about 2,000,000 segments), G = 64,
+distributions of the 1M x 64 sweep, seed 4; L = sum w . fine_flux + sum v . psi_out with
+w, v ~ N(0, 1)."""
+import numpy as np
+import pytest
+
+import mocatt
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+SEED = 4
+
+
+def loss_weights(hp, seed=SEED):
+    w = np.zeros((hp.R * hp.I, hp.Gs), np.float32)
+    v = np.zeros((hp.T, hp.Gs), np.float32)
+    w[:, :hp.G] = mocatt.synth_normal(seed, 6, hp.R * hp.I * hp.G).reshape(-1, hp.G)
+    v[:, :hp.G] = mocatt.synth_normal(seed, 7, hp.T * hp.G).reshape(-1, hp.G)
+    return w, v
+
+
+def gpu_adjoint(handle, hp, w, v):
+    import torch
+
+    dp = mocatt.DeviceProblem(hp)
+    wt = torch.from_numpy(w).cuda()
+    vt = torch.from_numpy(v).cuda()
+    ds, dsrc, dpsi = handle.adj(dp, wt, vt)
+    assert handle.synchronize() == 0
+    # the incoming psi is only read
+    np.testing.assert_array_equal(dp.to_host("psi"), hp.psi)
+    return ds.cpu().numpy(), dsrc.cpu().numpy(), dpsi.cpu().numpy()
+
+
+def rel(a, b, floor_frac=1e-3):
+    d = np.abs(a.astype(np.float64) - b)
+    den = np.maximum(np.abs(b), floor_frac * np.sqrt(np.mean(b * b)))
+    r = d / den
+    return float(r.max()), float(np.sqrt(np.mean(r * r)))
+
+
+@pytest.fixture(scope="module")
+def adj_problem():
+    hp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"])
+    w, v = loss_weights(hp)
+    return hp, w, v
+
+
+def test_adjoint_vs_fp64_cpu_adjoint(handle, adj_problem):
+    hp, w, v = adj_problem
+    assert 1.8e6 < hp.S < 2.2e6
+    ds, dsrc, dpsi = gpu_adjoint(handle, hp, w, v)
+    ref = oracle.adj_fp64(hp, w.astype(np.float64), v.astype(np.float64))
+    G = hp.G
+    out = {k: rel(a[:, :G], ref[r][:, :G]) for k, a, r in (
+        ("sigT", ds, "d_sigT"), ("source", dsrc, "d_source"), ("psi_in", dpsi, "d_psi_in"))}
+    print(out)
+    for k, (mx, rms) in out.items():
+        assert rms <= 1e-4, (k, mx, rms)
+        assert mx <= 1e-2, (k, mx, rms)
+
+
+def test_adjoint_vs_central_differences(handle, adj_problem):
+    """64 random parameters: GPU adjoint and FP64 adjoint vs FP64 central differences
+    (h = 1e-6) of the FP64 oracle's loss."""
+    hp, w, v = adj_problem
+    ds, dsrc, dpsi = gpu_adjoint(handle, hp, w, v)
+    w64, v64 = w.astype(np.float64), v.astype(np.float64)
+    sig = hp.sigT.astype(np.float64)
+    src = hp.source.astype(np.float64)
+    psi = hp.psi.astype(np.float64)
+    rng = np.random.default_rng(64)
+    h = 1e-6
+    worst = 0.0
+    for n in range(64):
+        kind = ("sigT", "source", "psi")[n % 3]
+        arr, grad = {"sigT": (sig, ds), "source": (src, dsrc), "psi": (psi, dpsi)}[kind]
+        i = int(rng.integers(arr.shape[0]))
+        g = int(rng.integers(hp.G))
+        args = {"sigT": sig, "source": src, "psi": psi}
+        lp_a, lm_a = dict(args), dict(args)
+        lp_a[kind] = arr.copy()
+        lm_a[kind] = arr.copy()
+        lp_a[kind][i, g] += h
+        lm_a[kind][i, g] -= h
+        lp = oracle.loss_fp64(hp, lp_a["sigT"], lp_a["source"], lp_a["psi"], w64, v64, g)
+        lm = oracle.loss_fp64(hp, lm_a["sigT"], lm_a["source"], lm_a["psi"], w64, v64, g)
+        fd = (lp - lm) / (2 * h)
+        noise = 64 * 2.0 ** -52 * max(abs(lp), abs(lm)) / h
+        err = abs(float(grad[i, g]) - fd) / max(abs(fd), 1.0)
+        worst = max(worst, err)
+        assert abs(float(grad[i, g]) - fd) <= 1e-3 * max(abs(fd), 1.0) + noise, \
+            (kind, i, g, float(grad[i, g]), fd)
+    print("worst relative deviation from central differences:", worst)
+
+
+def test_gradcheck_through_autograd_function(handle):
+    """A test-only torch.autograd.Function: forward = the FP64 oracle's loss
+    L(sigT, source, psi_in) for fixed w, v; backward = the GPU adjoint kernel
+    (moc_attenuate_adj). torch.autograd.gradcheck then compares the kernel's gradient
+    with FP64 central differences (h = 1e-6) of L, for every input entry of a small
+    problem. Tolerance 1e-3 relative: the kernel computes in FP32."""
+    import torch
+
+    hp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"].with_(
+        regions=3, groups=4, tracks=6, lognormal=(6.0, 0.5, 1, 20)))
+    w, v = loss_weights(hp, seed=9)
+    w64, v64 = w.astype(np.float64), v.astype(np.float64)
+
+    class SweepLoss(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, sig, src, psi_in):
+            ctx.save_for_backward(sig, src, psi_in)
+            L = oracle.loss_fp64(hp, sig.detach().cpu().numpy(), src.detach().cpu().numpy(),
+                                 psi_in.detach().cpu().numpy(), w64, v64)
+            return torch.tensor(L, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gL):
+            sig, src, psi_in = ctx.saved_tensors
+            q = hp.copy()
+            q.sigT = sig.detach().cpu().numpy().astype(np.float32)
+            q.source = src.detach().cpu().numpy().astype(np.float32)
+            q.psi = psi_in.detach().cpu().numpy().astype(np.float32)
+            ds, dsrc, dpsi = gpu_adjoint(handle, q, w, v)
+            g = float(gL)
+            return (torch.from_numpy(ds).double() * g, torch.from_numpy(dsrc).double() * g,
+                    torch.from_numpy(dpsi).double() * g)
+
+    # padding columns carry no gradient: check the real groups only
+    G = hp.G
+    sig = torch.from_numpy(hp.sigT.astype(np.float64)).requires_grad_()
+    src = torch.from_numpy(hp.source.astype(np.float64)).requires_grad_()
+    psi = torch.from_numpy(hp.psi.astype(np.float64)).requires_grad_()
+    assert hp.Gs == G  # G = 4: no padding
+    assert torch.autograd.gradcheck(SweepLoss.apply, (sig, src, psi), eps=1e-6, atol=1e-5,
+                                    rtol=1e-3)
+
+
+def test_adjoint_rejects_table_mode(handle):
+    import torch
+
+    hp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"].with_(
+        regions=3, groups=4, tracks=6, lognormal=(6.0, 0.5, 1, 20)))
+    dp = mocatt.DeviceProblem(hp)
+    w = torch.zeros_like(dp.fine_flux)
+    v = torch.zeros_like(dp.psi)
+    with pytest.raises(mocatt.MocError):
+        handle.adj(dp, w, v, mocatt.default_opts(exp_mode=mocatt.MOC_EXP_TABLE))

@@ -60,7 +60,7 @@ def test_noalloc_matches_handle_entry_point_twice(cuda, mode):
 
 def test_noalloc_rejects_oversize_and_bad_indices(cuda):
     big = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"].with_(
-        regions=3000, groups=128, tracks=4, segments=100))  # 3000*5*128*3 > 2,097,152
+        regions=3000, groups=128, tracks=4, segments=100))  # 3000*5*128 > 655,360
     assert _noalloc(mocatt.DeviceProblem(big), mocatt.default_opts()) == \
         mocatt.MOC_ERR_TOO_LARGE
     hp = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"].with_(regions=50, tracks=8,
