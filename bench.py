@@ -328,6 +328,8 @@ def gpu_arm(args, workload):
         "config": config_of(args, workload), "roofline": roof, "e2e": e2e,
         "gpu_launches": launches, "clocks": clk,
     }
+    if not args.no_forms and ws == 1:
+        line["forms"] = forms_section(h, dp, hp, sweep_s * 1e3)
     if not args.no_cpu_baseline and ws == 1:
         r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
                          args.table_points if args.exp == "table" else 0)
@@ -337,6 +339,117 @@ def gpu_arm(args, workload):
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _time_fwd(h, dp, opts, reps=3):
+    """Median device time of prep + sweep + finish over reps calls (after one warm-up)."""
+    h.fwd(dp, opts)
+    ts = []
+    for _ in range(reps):
+        h.fwd(dp, opts)
+        t = h.timings()
+        ts.append(t.prep_ms + t.sweep_ms + t.finish_ms)
+    if h.synchronize():
+        raise RuntimeError("device error")
+    return statistics.median(ts)
+
+
+FORMS_ACCURACY = os.path.join(ROOT, "profiles", "forms_accuracy_gb300.json")
+
+
+def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
+    """The three forms beside the plain sweep, timed on this GPU: the precision forms on the
+    bench workload (their accuracy against the FP64 oracle comes from the GPU test
+    tests/test_forms_gpu.py, recorded in profiles/forms_accuracy_gb300.json), the adjoint's
+    cost relative to one forward sweep, and the batching form against one launch per
+    problem."""
+    import ctypes as C
+
+    import torch
+
+    import mocatt
+
+    out = {}
+    plain = mocatt.default_opts(profile=1)
+    t_plain = _time_fwd(h, dp, plain)
+    accuracy = {}
+    if os.path.exists(FORMS_ACCURACY):
+        with open(FORMS_ACCURACY) as f:
+            accuracy = json.load(f)
+    forms = {
+        "plain_fp32": (mocatt.MOC_PREC_FP32, mocatt.MOC_TALLY_ATOMIC_FP32),
+        "fp32_stable": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_ATOMIC_FP32),
+        "fp32_stable_compensated": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_COMPENSATED),
+        "bf16_stable": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_ATOMIC_FP32),
+        "bf16_stable_compensated": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_COMPENSATED),
+        "fp16_stable": (mocatt.MOC_PREC_FP16, mocatt.MOC_TALLY_ATOMIC_FP32),
+    }
+    precision = {}
+    units = float(hp.S) * hp.G
+    for name, (prec, tally) in forms.items():
+        o = mocatt.default_opts(profile=1, precision=prec, tally=tally)
+        ms = t_plain if name == "plain_fp32" else _time_fwd(h, dp, o)
+        precision[name] = {"ms": ms, "value": units / (ms * 1e-3),
+                           "speed_vs_plain": t_plain / ms,
+                           "widetau_error": accuracy.get(name)}
+    ok = [n for n, v in precision.items() if n != "plain_fp32" and v["widetau_error"]
+          and v["widetau_error"]["psi"]["rms_rel"] <= 1e-5
+          and v["widetau_error"]["fine_flux"]["normwise"] <= 1e-5]
+    chosen = max(ok, key=lambda n: precision[n]["value"]) if ok else None
+    out["precision"] = precision
+    out["chosen_form"] = chosen
+    out["chosen_rule"] = ("fastest precision form whose psi RMS relative error is <= 1e-5 and "
+                          "whose fine_flux normwise error is <= 1e-5 against the FP64 oracle "
+                          "on the wide-tau inputs (tests/test_forms_gpu.py, recorded in "
+                          "profiles/forms_accuracy_gb300.json)")
+
+    # adjoint: 5,000 lognormal tracks, ~2M segments, G = 64
+    ahp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"])
+    adp = mocatt.DeviceProblem(ahp)
+    t_fwd = _time_fwd(h, adp, plain)
+    w = torch.randn_like(adp.fine_flux)
+    v = torch.randn_like(adp.psi)
+    h.adj(adp, w, v, plain)
+    ts = []
+    for _ in range(3):
+        h.adj(adp, w, v, plain)
+        t = h.timings()
+        ts.append(t.prep_ms + t.sweep_ms + t.finish_ms)
+    t_adj = statistics.median(ts)
+    out["adjoint"] = {"workload": "adjoint_2M_g64", "segments": ahp.S, "groups": ahp.G,
+                      "forward_ms": t_fwd, "adjoint_ms": t_adj, "ratio": t_adj / t_fwd}
+    del adp
+
+    # batching: three problems (G = 16, 70, 128), one graph-captured launch
+    bh = [mocatt.generate(mocatt.WORKLOADS[n])
+          for n in ("batch_20k_g16", "batch_20k_g70", "batch_20k_g128")]
+    bdp = [mocatt.DeviceProblem(x) for x in bh]
+    t_single = sum(_time_fwd(h, d, plain) for d in bdp)
+    arr = (mocatt.MocProblem * 3)(*[d.c_struct() for d in bdp])
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    res = mocatt.MocTuneResult()
+    h.check(mocatt.lib().moc_autotune_batch(h.ptr, arr, 3, C.byref(plain), sp, C.byref(res)))
+    h.check(mocatt.lib().moc_attenuate_fwd_batch(h.ptr, arr, 3, C.byref(plain), sp))
+    bt = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.check(mocatt.lib().moc_attenuate_fwd_batch(h.ptr, arr, 3, C.byref(plain), sp))
+        e1.record(stream)
+        e1.synchronize()
+        bt.append(e0.elapsed_time(e1))
+    if h.synchronize():
+        raise RuntimeError("device error")
+    t_batch = statistics.median(bt)
+    bunits = sum(float(x.S) * x.G for x in bh)
+    out["batching"] = {"problems": [{"G": x.G, "tracks": x.T, "segments": x.S} for x in bh],
+                       "one_launch_ms": t_batch, "three_calls_ms": t_single,
+                       "value": bunits / (t_batch * 1e-3), "speedup": t_single / t_batch,
+                       "tuned": {"vec": res.vec, "warps_per_block": res.warps_per_block,
+                                 "tracks_per_block": res.tracks_per_block}}
+    return out
 
 
 def main():
@@ -351,6 +464,8 @@ def main():
     ap.add_argument("--cpu-sample-tracks", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the precision / adjoint / batching measurements")
     ap.add_argument("--segments", type=int, default=0,
                     help="override the workload's segment count (smaller profiling cases)")
     ap.add_argument("--tracks", type=int, default=0, help="override the track count")

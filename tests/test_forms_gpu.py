@@ -95,6 +95,47 @@ def test_compensated_tally_is_correctly_rounded():
     assert out["comp"] < out["f32"] / 4
 
 
+REPORT_FORMS = {
+    "plain_fp32": (mocatt.MOC_PREC_FP32, mocatt.MOC_TALLY_ATOMIC_FP32),
+    "fp32_stable": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_ATOMIC_FP32),
+    "fp32_stable_compensated": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_COMPENSATED),
+    "bf16_stable": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_ATOMIC_FP32),
+    "bf16_stable_compensated": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_COMPENSATED),
+    "fp16_stable": (mocatt.MOC_PREC_FP16, mocatt.MOC_TALLY_ATOMIC_FP32),
+}
+
+
+def test_forms_accuracy_report(handle):
+    """Error of every form bench.py times, on the wide-tau inputs, against the FP64 oracle
+    on the values the form stores. With MOC_FORMS_REPORT=<path> the numbers are written
+    there as JSON (bench.py reports them beside its timings)."""
+    import json
+    import os
+
+    hp = widetau()
+    report_all = {}
+    for name, (prec, tally) in REPORT_FORMS.items():
+        psi, ff = run(handle, hp, mocatt.default_opts(precision=prec, tally=tally))
+        if prec == mocatt.MOC_PREC_FP32:
+            ref = oracle.fwd_fp64(hp)
+        else:
+            qp, coef = oracle.quantized_inputs(hp, prec)
+            ref = oracle.fwd_fp64_coef(qp, coef)
+        rep = report(hp, psi, ff, ref)
+        report_all[name] = {k: {"max_rel": v[0], "rms_rel": v[1], "normwise": v[2]}
+                            for k, v in (("psi", rep["psi"]), ("fine_flux", rep["ff"]))}
+    report_all["inputs"] = ("widetau_50M_g128 shapes cut to 200,000 segments, 400 tracks, "
+                            "400 regions (sigT ~ logU(1e-3, 20), ds ~ U(1e-3, 2)); FP64 oracle "
+                            "on the stored (rounded) sigT and coefficients; relative error "
+                            "floor 1e-6 of the RMS")
+    print(json.dumps(report_all, indent=1))
+    path = os.environ.get("MOC_FORMS_REPORT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(report_all, f, indent=1)
+    assert report_all["fp32_stable"]["psi"]["rms_rel"] < report_all["plain_fp32"]["psi"]["rms_rel"]
+
+
 def test_precision_forms_reject_table_mode(handle):
     hp = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"].with_(regions=20, tracks=4,
                                                                  segments=100))
