@@ -45,21 +45,25 @@ UNIT = "segment·group attenuations/s"
 PEAKS_FILE = os.path.join(ROOT, "profiles", "peaks_gb300.json")
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
-# Algorithmic L2 bytes per segment*group of the plain FP32 sweep at G=128, I=5:
-# sigT row 4 B + axial-coefficient rows (3 rows for interior intervals, 2 at the ends:
-# (3*3 + 2*2)/5 * 4 B = 10.4 B) + tally reduction 4 B + descriptor 9 B / 128 groups.
+# Algorithmic L2 bytes per segment*group of the plain FP32 sweep: the cell block
+# (sigT, q0, q1*mu, q2*mu2) 16 B + the segment descriptor 9 B / G gathered, and the tally
+# 4 B reduced. FP32 instructions per segment*group of the plain arithmetic (27, counted
+# from attenuate<> in csrc/moc_sweep.cu) and MUFU operations (ex2 + rcp).
+FP32_OPS_PER_UNIT = 27
+MUFU_OPS_PER_UNIT = 2
+
+
 def l2_bytes_per_unit(I: int, G: int) -> dict:
-    rows = (3 * (I - 2) + 2 * 2) / I
-    return {"gather": 4.0 + 4.0 * rows + 9.0 / G, "reduce": 4.0}
+    return {"gather": 16.0 + 9.0 / G, "reduce": 4.0}
 
 
 def hbm_compulsory_bytes(hp) -> float:
     """Bytes a sweep must move to or from HBM at least once: descriptors, offsets, psi in
-    and out, sigT, source (read by the coefficient pass), coefficients written and read,
+    and out, sigT and source (read by the block pass), cell blocks written and read,
     fine_flux read and written."""
     S, T, Gs, R, I = hp.S, hp.T, hp.Gs, hp.R, hp.I
     return (9.0 * S + 8.0 * (T + 1) + 2 * 4.0 * T * Gs + 4.0 * R * Gs + 4.0 * R * I * Gs
-            + 2 * 12.0 * R * I * Gs + 2 * 4.0 * R * I * Gs)
+            + 2 * 16.0 * R * I * Gs + 2 * 4.0 * R * I * Gs)
 
 
 def dist_env():
@@ -151,13 +155,16 @@ def load_peaks() -> dict:
 def run_peaks() -> dict:
     lib = C.CDLL(os.path.join(PKG, "_build", "libmocpeaks.so"))
     lib.mocpeak_run.restype = C.c_int
-    res = (C.c_double * 6)()
-    rc = lib.mocpeak_run(res, 6)
+    res = (C.c_double * 9)()
+    rc = lib.mocpeak_run(res, 9)
     if rc:
         raise RuntimeError(f"mocpeak_run failed: {rc}")
-    out = {"l2_stream_read_gbs": res[0], "l2_row_gather_gbs": res[1],
-           "l2_row_reduce_gbs": res[2], "fp32_fma_tflops": res[3], "mufu_ex2_gops": res[4],
-           "hbm_read_gbs": res[5],
+    out = {"l2_stream_read_gbs": res[0], "l2_row_gather_hashed_gbs": res[1],
+           "l2_row_reduce_hashed_gbs": res[2], "fp32_fma_tflops": res[3],
+           "mufu_ex2_gops": res[4], "hbm_read_gbs": res[5], "l2_row_gather_gbs": res[6],
+           "l2_row_reduce_gbs": res[7], "l2_mix_gbs": res[8],
+           "mix": "four random 512-byte row gathers per 512-byte red.v4 row reduction "
+                  "(the sweep's 16 B gathered : 4 B reduced per segment*group)",
            "how": "simplemoc-kernel_gb300/csrc/moc_peaks.cu via bench.py --peaks: "
                   "CUDA events, mean of 5 launches after 1 warm-up"}
     return out
@@ -293,24 +300,27 @@ def gpu_arm(args, workload):
             "algorithmic_bytes_per_unit": per["gather"] + per["reduce"],
             "units_per_launch": units, "sweep_ms": sweep_s * 1e3,
             "prep_ms": statistics.mean(prep_ms), "traffic": None}
-    if "l2_row_gather_gbs" in peaks:
-        t_l2 = (per["gather"] * units / (peaks["l2_row_gather_gbs"] * 1e9) +
-                per["reduce"] * units / (peaks["l2_row_reduce_gbs"] * 1e9))
-        roof["peak"] = l2_bytes / t_l2 / 1e9
-        roof["peak_source"] = ("profiles/peaks_gb300.json: random 512-byte row gathers and "
-                               "red.v4 row reductions into L2-resident tables, combined in "
-                               "the sweep's byte mix")
-        roof["frac"] = roof["achieved"] / roof["peak"]
-        terms = {"l2": t_l2 * 1e3,
-                 "mufu": 2 * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3,
-                 "fp32": 34 * units / (peaks["fp32_fma_tflops"] * 1e12 / 2) * 1e3}
-    else:
-        roof["peak"] = None
-        roof["frac"] = None
-        terms = {}
+    terms = {}
+    if "l2_mix_gbs" in peaks:
+        # every resource the sweep needs, at its measured peak; the largest time binds
+        terms["l2"] = l2_bytes / (peaks["l2_mix_gbs"] * 1e9) * 1e3
+        terms["fp32"] = FP32_OPS_PER_UNIT * units / (peaks["fp32_fma_tflops"] * 1e12 / 2) * 1e3
+        terms["mufu"] = MUFU_OPS_PER_UNIT * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3
+        roof["peak"] = peaks["l2_mix_gbs"]
+        roof["peak_source"] = ("profiles/peaks_gb300.json l2_mix_gbs: random 512-byte row "
+                               "gathers and red.v4 row reductions in the sweep's 4:1 byte mix "
+                               "(bench.py --peaks, csrc/moc_peaks.cu)")
     hbm_bytes = hbm_compulsory_bytes(hp)
     terms["hbm"] = hbm_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
     roof["terms_ms"] = terms
+    binding = max(terms, key=terms.get)
+    roof["binding_term"] = binding
+    roof["binding_frac"] = terms[binding] / (sweep_s * 1e3)
+    if roof.get("peak"):
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    else:
+        roof["peak"] = None
+        roof["frac"] = None
     roof["hbm"] = {"compulsory_bytes": hbm_bytes, "achieved_gbs": hbm_bytes / sweep_s / 1e9,
                    "peak_gbs": peaks["hbm_gbs"], "frac": hbm_bytes / sweep_s / 1e9 / peaks["hbm_gbs"],
                    "peak_source": peaks["hbm_source"]}

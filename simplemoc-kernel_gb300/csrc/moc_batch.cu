@@ -127,17 +127,18 @@ __device__ __forceinline__ void attenuate_b(const float4 (&x)[VEC], float ds, fl
             p = ex2_approx(tau * -1.44269504088896341f);
             e = 1.0f - p;
         }
+        // same arithmetic as the single-problem sweep (attenuate<> in moc_sweep.cu)
         const float tme = tau - e;
-        const float cub = tau * (tau * (tau - 3.0f) + 6.0f) - 6.0f * e;
+        const float cub = fmaf(tau * tau, tau - 3.0f, 6.0f * tme);
         const float rs = rcp_approx(s);
         const float rs2 = rs * rs;
-        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * e * (rs * rs2));
-        float fi = (fmaf(s, ps, -a0) * e + a0 * tau) * rs2;
+        const float e1 = e * rs, t2 = tme * rs2;
+        const float reuse = fmaf(e1 + e1, rs2, tau * (tau - 2.0f));
+        float fi = fmaf(a0, t2, ps * e1);
         fi = fmaf(a1, reuse, fi);
         fi = fmaf(a2 * cub, rs2 * rs2 * (1.0f / 3.0f), fi);
         tally.v[k] = weight * fi;
-        float pn = a0 * e * rs;
-        pn = fmaf(a1 * tme, rs2, pn);
+        float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);
         psi.v[k] = fmaf(ps, p, pn);
     }

@@ -68,6 +68,48 @@ __global__ void row_reduce(float *ff, uint32_t n_rows, int iters)
     }
 }
 
+// Lean variants: rows drawn by a 32-bit LCG over a power-of-two row count (two integer
+// operations per row), four independent streams per warp for memory-level parallelism,
+// so the issue of the loop itself does not limit the L2.
+//   mode 0: gathers only; 1: reductions only; 2: four gathers per reduction (the sweep's
+//   byte mix: a 16-byte cell block per group read, a 4-byte tally per group reduced).
+__global__ void row_mix(const float4 *__restrict__ rows, float *ff, int log2_rows,
+                        int log2_ff_rows, int iters, int mode, float *out)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t s0 = hash32(warp * 4 + 1), s1 = hash32(warp * 4 + 2), s2 = hash32(warp * 4 + 3),
+             s3 = hash32(warp * 4 + 4);
+    const int sh = 32 - log2_rows, shf = 32 - log2_ff_rows;
+    float acc = 0.0f;
+    for (int i = 0; i < iters; i++) {
+        s0 = s0 * 1664525u + 1013904223u;
+        s1 = s1 * 1664525u + 1013904223u;
+        s2 = s2 * 1664525u + 1013904223u;
+        s3 = s3 * 1664525u + 1013904223u;
+        if (mode != 1) {
+            const float4 a = __ldg(rows + (size_t)(s0 >> sh) * 32 + lane);
+            const float4 b = __ldg(rows + (size_t)(s1 >> sh) * 32 + lane);
+            const float4 c = __ldg(rows + (size_t)(s2 >> sh) * 32 + lane);
+            const float4 d = __ldg(rows + (size_t)(s3 >> sh) * 32 + lane);
+            acc += (a.x + b.y) + (c.z + d.w);
+        }
+        if (mode != 0) {
+            float *p = ff + (size_t)(s0 >> shf) * 128 + lane * 4;
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(1.0f),
+                         "f"(1.0f), "f"(1.0f), "f"(1.0f)
+                         : "memory");
+            if (mode == 1) {
+                float *q = ff + (size_t)(s1 >> shf) * 128 + lane * 4;
+                asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(q),
+                             "f"(1.0f), "f"(1.0f), "f"(1.0f), "f"(1.0f)
+                             : "memory");
+            }
+        }
+    }
+    if (acc == 1234.5f) out[warp] = acc;
+}
+
 __global__ void fma_chains(float *out, int iters, float a, float b)
 {
     float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
@@ -156,6 +198,18 @@ extern "C" int mocpeak_run(double *res, int n_res)
 
     ms = time_ms([&] { stream_read<<<blocks, threads>>>((const float4 *)hbm, hbm_bytes / 16, 1, out, 1); }, 5);
     res[5] = (double)hbm_bytes / (ms * 1e-3) / 1e9;
+
+    if (n_res >= 9) {
+        // 2^17 rows of 512 B (64 MiB) to gather from, 2^15 tally rows (16 MiB) to reduce into
+        const int lr = 17, lf = 15, it = 2000;
+        const double warps = (double)blocks * (threads / 32);
+        ms = time_ms([&] { row_mix<<<blocks, threads>>>((const float4 *)rows, ff, lr, lf, it, 0, out); }, 5);
+        res[6] = warps * it * 4 * 512.0 / (ms * 1e-3) / 1e9;
+        ms = time_ms([&] { row_mix<<<blocks, threads>>>((const float4 *)rows, ff, lr, lf, it, 1, out); }, 5);
+        res[7] = warps * it * 2 * 512.0 / (ms * 1e-3) / 1e9;
+        ms = time_ms([&] { row_mix<<<blocks, threads>>>((const float4 *)rows, ff, lr, lf, it, 2, out); }, 5);
+        res[8] = warps * it * 5 * 512.0 / (ms * 1e-3) / 1e9;
+    }
 
     const cudaError_t e = cudaDeviceSynchronize();
     cudaFree(out);

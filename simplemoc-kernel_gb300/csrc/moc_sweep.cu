@@ -164,38 +164,35 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
         const float ps = psi.v[k];
         const float tau = __fmul_rn(s, ds);  // kept exact: the table index depends on it
         float e, p, tme, cub;
-        if constexpr (EK == EXPK_TABLE) {
-            e = table_lookup(tr.tab, tr.n, tr.dx, tr.max, tau);
-            p = 1.0f - e;
-            tme = tau - e;
-            cub = tau * (tau * (tau - 3.0f) + 6.0f) - 6.0f * e;
-        } else if constexpr (EK == EXPK_PLAIN) {
-            p = ex2_approx(tau * -1.44269504088896341f);
-            e = 1.0f - p;
-            tme = tau - e;
-            cub = tau * (tau * (tau - 3.0f) + 6.0f) - 6.0f * e;
-        } else {
+        if constexpr (EK == EXPK_STABLE) {
             const ExpTerms x = exp_terms_stable(tau);
             e = x.e;
             p = x.p;
             tme = x.tme;
             cub = x.cub;
+        } else {
+            if constexpr (EK == EXPK_TABLE) {
+                e = table_lookup(tr.tab, tr.n, tr.dx, tr.max, tau);
+                p = 1.0f - e;
+            } else {
+                p = ex2_approx(tau * -1.44269504088896341f);
+                e = 1.0f - p;
+            }
+            tme = tau - e;
+            // tau(tau(tau-3)+6) - 6e = tau^2 (tau - 3) + 6 (tau - e)
+            cub = fmaf(tau * tau, tau - 3.0f, 6.0f * tme);
         }
+        // (q0 tau + (s psi - q0) e)/s^2 == q0 (tau - e)/s^2 + psi e/s exactly, so FI and
+        // psi' share e/s and (tau - e)/s^2; 2e/s^3 = 2 (e/s) / s^2.
         const float rs = rcp_approx(s);
         const float rs2 = rs * rs;
-        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * e * (rs * rs2));
-        float fi;
-        if constexpr (EK == EXPK_STABLE) {
-            // (q0 tau + (s psi - q0) e)/s^2 == q0 (tau - e)/s^2 + psi e/s, exactly
-            fi = fmaf(a0 * tme, rs2, ps * e * rs);
-        } else {
-            fi = (fmaf(s, ps, -a0) * e + a0 * tau) * rs2;
-        }
+        const float e1 = e * rs, t2 = tme * rs2;
+        const float reuse = fmaf(e1 + e1, rs2, tau * (tau - 2.0f));
+        float fi = fmaf(a0, t2, ps * e1);
         fi = fmaf(a1, reuse, fi);
         fi = fmaf(a2 * cub, rs2 * rs2 * (1.0f / 3.0f), fi);
         tally.v[k] = weight * fi;
-        float pn = a0 * e * rs;
-        pn = fmaf(a1 * tme, rs2, pn);
+        float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);
         psi.v[k] = fmaf(ps, p, pn);
     }
