@@ -136,7 +136,11 @@ typedef struct {
     int32_t warps_per_block;      /* 0 = auto, else 1..8                                */
     int32_t profile;              /* 1: time each kernel of the call with CUDA events on
                                      the call's stream (read with moc_last_timings)      */
-    int32_t reserved[3];
+    int32_t prefetch;             /* segments whose cell blocks are in flight ahead of the
+                                     arithmetic: 0 = auto, 1 = one (registers), 8 = seven,
+                                     through a cp.async ring in shared memory (plain and
+                                     stable FP32 forms with FP32 tallies)                  */
+    int32_t reserved[2];
 } moc_fwd_opts_t;
 
 /* Device time of each kernel of the last call made with opts.profile = 1. */

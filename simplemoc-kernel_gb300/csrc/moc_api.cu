@@ -107,6 +107,12 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         return MOC_ERR_INVALID_ARG;
     if (o->vec != 0 && o->vec != 1 && o->vec != 2 && o->vec != 4) return MOC_ERR_INVALID_ARG;
     if (o->warps_per_block < 0 || o->warps_per_block > 8) return MOC_ERR_INVALID_ARG;
+    if (o->prefetch != 0 && o->prefetch != 1 && o->prefetch != moc::RING_DEPTH)
+        return MOC_ERR_INVALID_ARG;
+    if (o->prefetch == moc::RING_DEPTH &&
+        (o->precision == MOC_PREC_BF16 || o->precision == MOC_PREC_FP16 ||
+         o->tally != MOC_TALLY_ATOMIC_FP32))
+        return MOC_ERR_UNSUPPORTED;
     if (!std::isfinite(o->dz) || o->dz == 0.0f) return MOC_ERR_INVALID_ARG;
     // The precision forms use the accurate exponential; the table is the plain form's.
     if (o->exp_mode == MOC_EXP_TABLE && o->precision != MOC_PREC_FP32)
@@ -184,8 +190,8 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
                    : o->tally == MOC_TALLY_FP64      ? moc::TALLY_F64
                                                      : moc::TALLY_F32;
     }
-    const size_t smem = c->exp_kind == moc::EXPK_TABLE ? (size_t)o->table_points * 8 : 0;
-    const int per_sm = moc::fwd_blocks_per_sm(*c, smem);
+    c->prefetch = o->prefetch > 1 ? o->prefetch : 1;
+    const int per_sm = moc::fwd_blocks_per_sm(*c, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
     c->blocks = per_sm * h->sm_count;
     return MOC_OK;

@@ -77,6 +77,24 @@ __device__ __forceinline__ void st_psi(float *p, const Vec<VEC> &r, int n_valid)
     }
 }
 
+// Asynchronous 16-byte global -> shared copy through L2 only (cp.async.cg), and its
+// commit / wait (the wait count is a compile-time constant).
+__device__ __forceinline__ void cp_async16(float4 *smem_dst, const float4 *gmem_src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem_src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Streaming load of a per-segment descriptor field (read once; evict first).
 template <typename T>
 __device__ __forceinline__ T ld_stream(const T *p)

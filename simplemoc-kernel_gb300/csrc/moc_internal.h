@@ -77,6 +77,7 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
                           cudaStream_t st);
 
 // The forward sweep (persistent, one warp per (track, group chunk) work item).
+constexpr int RING_DEPTH = 8;  // depth of the shared-memory prefetch ring
 struct FwdConfig {
     int vec;              // groups per lane: 1, 2, 4
     int warps_per_block;  // 1..8
@@ -84,13 +85,16 @@ struct FwdConfig {
     int blocks;           // grid size (0 = fill the GPU)
     int store = STORE_F32;
     int tally = TALLY_F32;
+    int prefetch = 1;     // 1: registers, one segment ahead; RING_DEPTH: cp.async ring
 };
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &cfg, cudaStream_t st);
+// Dynamic shared memory of a configuration (table of tab_n pairs in table mode + rings).
+size_t fwd_smem_bytes(const FwdConfig &cfg, int tab_n);
 // Default groups per lane for G groups (measured fastest at G = 64 and 128 on GB300:
 // two groups per lane keeps registers low enough for 32 resident warps per SM).
 inline int auto_vec(int G) { return G > 32 ? 2 : 1; }
 // Resident blocks per SM for a configuration (0 if the configuration is invalid).
-int fwd_blocks_per_sm(const FwdConfig &cfg, size_t smem_bytes);
+int fwd_blocks_per_sm(const FwdConfig &cfg, int tab_n);
 
 // Checked mode: scan offsets and segment indices, OR errors into p.err. No writes
 // to psi or fine_flux.

@@ -147,8 +147,8 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     cfg.vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
     cfg.warps_per_block = o->warps_per_block ? o->warps_per_block : 8;
     cfg.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
-    const size_t smem = cfg.exp_kind == moc::EXPK_TABLE ? (size_t)o->table_points * 8 : 0;
-    const int per_sm = moc::fwd_blocks_per_sm(cfg, smem);
+    cfg.prefetch = o->prefetch > 1 ? o->prefetch : 1;
+    const int per_sm = moc::fwd_blocks_per_sm(cfg, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
     cfg.blocks = per_sm * sms;
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);

@@ -216,9 +216,9 @@ __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t 
     }
 }
 
-template <int VEC, int EK, int ST, int TL>
+template <int VEC, int EK, int ST, int TL, int RD>
 __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int lane,
-                                           const TableRef &tr)
+                                           const TableRef &tr, float4 *ring)
 {
     const int t = (int)(item / P.n_chunks);
     const int ch = (int)(item - (int64_t)t * P.n_chunks);
@@ -267,40 +267,105 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         }
     };
 
-    Blk<VEC> b0, b1;
-    int c0 = -1, c1 = -1;
-    float d0 = 0.0f, d1 = 0.0f;
-    if (beg < end) {
-        desc(beg, c0, d0);
-        if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
-    }
-    for (int64_t j = beg; j < end; j += 2) {
-        const bool has1 = j + 1 < end;
-        if (has1) {
-            desc(j + 1, c1, d1);
-            if (c1 >= 0 && act) load_blk<VEC, ST>(P.blk, c1 * Gs + g0, b1);
-        }
-        step(b0, c0, d0);
-        if (!has1) break;
-        if (j + 2 < end) {
-            desc(j + 2, c0, d0);
+    if constexpr (RD == 0) {
+        // one segment ahead, in registers (ping-pong, no moves)
+        Blk<VEC> b0, b1;
+        int c0 = -1, c1 = -1;
+        float d0 = 0.0f, d1 = 0.0f;
+        if (beg < end) {
+            desc(beg, c0, d0);
             if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
         }
-        step(b1, c1, d1);
+        for (int64_t j = beg; j < end; j += 2) {
+            const bool has1 = j + 1 < end;
+            if (has1) {
+                desc(j + 1, c1, d1);
+                if (c1 >= 0 && act) load_blk<VEC, ST>(P.blk, c1 * Gs + g0, b1);
+            }
+            step(b0, c0, d0);
+            if (!has1) break;
+            if (j + 2 < end) {
+                desc(j + 2, c0, d0);
+                if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+            }
+            step(b1, c1, d1);
+        }
+    } else {
+        // RD - 1 segments ahead, through a per-warp ring in shared memory filled by
+        // cp.async: ring[(slot * VEC + v) * 32 + lane] holds group g0 + v of the segment
+        // in that slot. Each lane reads only what it copied, so the wait on its own copy
+        // groups is the only synchronisation. The issue pointer runs RD - 1 segments
+        // ahead of the compute pointer, inside descriptor windows A and B.
+        static_assert(ST == STORE_F32 && (RD & (RD - 1)) == 0 && RD <= 16, "ring");
+        auto peek = [&](int64_t jj, int &c, float &d) {
+            const int k = (int)(jj - wb);
+            if (k < 32) {
+                c = __shfl_sync(FULL, cA, k);
+                d = __shfl_sync(FULL, dA, k);
+            } else {
+                c = __shfl_sync(FULL, cB, k - 32);
+                d = __shfl_sync(FULL, dB, k - 32);
+            }
+        };
+        const float4 *blk = static_cast<const float4 *>(P.blk) + g0;
+        auto issue = [&](int64_t jj, int slot) {
+            if (jj < end) {
+                int c;
+                float d;
+                peek(jj, c, d);
+                if (c >= 0 && act) {
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        cp_async16(ring + (slot * VEC + v) * 32 + lane, blk + c * Gs + v);
+                }
+            }
+            cp_async_commit();
+        };
+#pragma unroll
+        for (int s = 0; s < RD - 1; s++) issue(beg + s, s);
+        for (int64_t j = beg; j < end; j++) {
+            if (j - wb == 32) {
+                cA = cB;
+                dA = dB;
+                wb += 32;
+                decode(P, wb + 32 + lane, end, cB, dB);
+            }
+            const int slot = (int)((j - beg) & (RD - 1));
+            issue(j + RD - 1, (slot + RD - 1) & (RD - 1));
+            cp_async_wait<RD - 1>();
+            int c;
+            float d;
+            peek(j, c, d);
+            if (c >= 0 && act) {
+                Blk<VEC> b;
+#pragma unroll
+                for (int v = 0; v < VEC; v++) b.v[v] = ring[(slot * VEC + v) * 32 + lane];
+                step(b, c, d);
+            }
+        }
+        cp_async_wait<0>();
     }
     if (act) st_psi<VEC>(psi_row, psi, nvalid);
 }
 
-template <int VEC, int EK, int ST, int TL>
+// Dynamic shared memory: the exponential table (table mode), then one prefetch ring of
+// RD * VEC * 32 float4 per warp.
+template <int VEC, int EK, int ST, int TL, int RD>
 __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
 {
-    extern __shared__ float2 s_tab[];
+    extern __shared__ float4 s_dyn[];
     TableRef tr{nullptr, 0, 0.0f, 0.0f};
+    float2 *s_tab = reinterpret_cast<float2 *>(s_dyn);
     if constexpr (EK == EXPK_TABLE) {
         const float2 *src = reinterpret_cast<const float2 *>(P.table);
         for (int k = threadIdx.x; k < P.tab_n; k += blockDim.x) s_tab[k] = src[k];
         __syncthreads();
         tr = TableRef{s_tab, P.tab_n, P.tab_dx, P.tab_max};
+    }
+    float4 *ring = nullptr;
+    if constexpr (RD > 0) {
+        const int tab_f4 = EK == EXPK_TABLE ? (P.tab_n + 1) / 2 : 0;
+        ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD * VEC * 32);
     }
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -308,7 +373,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)P.n_items) break;
-        sweep_item<VEC, EK, ST, TL>(P, (int64_t)item, lane, tr);
+        sweep_item<VEC, EK, ST, TL, RD>(P, (int64_t)item, lane, tr, ring);
     }
 }
 
@@ -340,19 +405,28 @@ __global__ void finish_kernel(float *__restrict__ ff, const float *__restrict__ 
     }
 }
 
-template <int VEC, int EK, int ST, int TL>
+template <int VEC, int EK, int ST, int TL, int RD = 0>
 const void *fwd_fn()
 {
-    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL>);
+    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD>);
 }
 
-// The instantiated (exp, storage, tally) combinations, for every VEC:
-//   plain FP32 / table FP32 with FP32 atomics (the drop-in),
-//   stable math with FP32 storage and all three tally kinds,
-//   stable math with BF16 / FP16 storage and all three tally kinds.
+// The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
+//   plain FP32 / table FP32 with FP32 atomics (the drop-in), register or ring prefetch,
+//   stable math with FP32 storage and all three tally kinds (FP32 tallies also with the
+//   ring), stable math with BF16 / FP16 storage and all three tally kinds.
 template <int V>
 const void *pick_vec(const FwdConfig &c)
 {
+    if (c.prefetch > 1) {
+        if (c.prefetch != RING_DEPTH || c.store != STORE_F32 || c.tally != TALLY_F32)
+            return nullptr;
+        if (c.exp_kind == EXPK_PLAIN)
+            return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, RING_DEPTH>();
+        if (c.exp_kind == EXPK_TABLE)
+            return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, RING_DEPTH>();
+        return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, RING_DEPTH>();
+    }
     if (c.store == STORE_F32) {
         if (c.exp_kind == EXPK_PLAIN && c.tally == TALLY_F32)
             return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>();
@@ -432,10 +506,19 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
     return cudaGetLastError();
 }
 
-int fwd_blocks_per_sm(const FwdConfig &c, size_t smem)
+size_t fwd_smem_bytes(const FwdConfig &c, int tab_n)
+{
+    size_t b = c.exp_kind == EXPK_TABLE ? (size_t)(tab_n + 1) / 2 * sizeof(float4) : 0;
+    if (c.prefetch > 1)
+        b += (size_t)c.warps_per_block * c.prefetch * c.vec * 32 * sizeof(float4);
+    return b;
+}
+
+int fwd_blocks_per_sm(const FwdConfig &c, int tab_n)
 {
     const void *fn = pick(c);
     if (!fn || c.warps_per_block < 1 || c.warps_per_block > 8) return 0;
+    const size_t smem = fwd_smem_bytes(c, tab_n);
     int n = 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
@@ -451,7 +534,7 @@ cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &c, cudaStream_t st
     const void *fn = pick(c);
     if (!fn || c.warps_per_block < 1 || c.warps_per_block > 8 || c.blocks < 1)
         return cudaErrorInvalidValue;
-    const size_t smem = c.exp_kind == EXPK_TABLE ? (size_t)p.tab_n * sizeof(float2) : 0;
+    const size_t smem = fwd_smem_bytes(c, p.tab_n);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

@@ -65,7 +65,7 @@ class MocFwdOpts(C.Structure):
         ("dz", C.c_float), ("zin", C.c_float), ("weight", C.c_float), ("mu", C.c_float),
         ("mu2", C.c_float), ("checked", C.c_int32), ("vec", C.c_int32),
         ("warps_per_block", C.c_int32), ("profile", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("prefetch", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 

@@ -137,8 +137,9 @@ def test_gradcheck_through_autograd_function(handle):
     src = torch.from_numpy(hp.source.astype(np.float64)).requires_grad_()
     psi = torch.from_numpy(hp.psi.astype(np.float64)).requires_grad_()
     assert hp.Gs == G  # G = 4: no padding
+    # the kernel's FP32 atomic accumulation order varies between runs: nondet_tol
     assert torch.autograd.gradcheck(SweepLoss.apply, (sig, src, psi), eps=1e-6, atol=1e-5,
-                                    rtol=1e-3)
+                                    rtol=1e-3, nondet_tol=1e-3)
 
 
 def test_adjoint_rejects_table_mode(handle):

@@ -47,10 +47,35 @@ def test_plain_group_counts(handle, G):
 
 @pytest.mark.parametrize("vec", [1, 2, 4])
 @pytest.mark.parametrize("wpb", [1, 4, 8])
-def test_plain_launch_shapes(handle, vec, wpb):
+@pytest.mark.parametrize("prefetch", [1, 8])
+def test_plain_launch_shapes(handle, vec, wpb, prefetch):
     hp = small(groups=64)
-    psi, ff = run_gpu(handle, hp, mocatt.default_opts(vec=vec, warps_per_block=wpb))
+    opts = mocatt.default_opts(vec=vec, warps_per_block=wpb, prefetch=prefetch)
+    psi, ff = run_gpu(handle, hp, opts)
     parity.check_plain(psi, ff, oracle.fwd_fp64(hp), hp.G)
+
+
+@pytest.mark.parametrize("G", [3, 70, 128])
+def test_prefetch_ring_matches_registers(handle, G):
+    """The shared-memory prefetch ring computes exactly what the register path computes:
+    psi bit for bit, including ragged tracks and out-of-range segments (skipped)."""
+    hp = small(groups=G, tracks=300, segments=9000)
+    hp.seg_region[17] = hp.R + 3
+    p1, f1 = run_gpu_unchecked(handle, hp, mocatt.default_opts(prefetch=1))
+    p8, f8 = run_gpu_unchecked(handle, hp, mocatt.default_opts(prefetch=8))
+    assert np.array_equal(p1, p8)
+    tab = dict(exp_mode=mocatt.MOC_EXP_TABLE, table_points=10_000)
+    p1, _ = run_gpu_unchecked(handle, hp, mocatt.default_opts(prefetch=1, **tab))
+    p8, _ = run_gpu_unchecked(handle, hp, mocatt.default_opts(prefetch=8, **tab))
+    assert np.array_equal(p1, p8)
+
+
+def run_gpu_unchecked(handle, hp, opts):
+    """Run and expect exactly the bad-index report of a planted out-of-range segment."""
+    dp = mocatt.DeviceProblem(hp)
+    handle.fwd(dp, opts)
+    assert handle.synchronize() == mocatt.MOC_ERR_BAD_INDEX
+    return dp.to_host("psi"), dp.to_host("fine_flux")
 
 
 @pytest.mark.parametrize("npts,maxv", [(353, 10.0), (10_000, 10.0), (50, 3.0)])
