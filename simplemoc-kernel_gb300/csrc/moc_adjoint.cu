@@ -136,6 +136,15 @@ __device__ __forceinline__ bool item_range(const SweepParams &P, int64_t item, i
     return true;
 }
 
+// One segment's inputs for the reverse sweep, fetched one segment ahead.
+template <int VEC>
+struct RevSeg {
+    int c;
+    float d;
+    float4 b[VEC];
+    Vec<VEC> psi, w;
+};
+
 template <int VEC>
 __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
 {
@@ -155,21 +164,47 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
         const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
         Vec<VEC> psi;
         if (act) psi = ld_psi<VEC>(P.psi + (int64_t)t * Gs + g0, nvalid);
-        for (int64_t wb = beg; wb < end; wb += 32) {
-            int cw;
-            float dw;
-            decode(P, wb + lane, beg, end, cw, dw);
-            const int n = end - wb < 32 ? (int)(end - wb) : 32;
-            for (int k = 0; k < n; k++) {
-                const int c = __shfl_sync(FULL, cw, k);
-                const float d = __shfl_sync(FULL, dw, k);
-                if (!act) continue;
-                st_psi<VEC>(A.hist + (wb + k) * Gs + g0, psi, nvalid);
-                if (c < 0) continue;
-                float4 b[VEC];
-                load4<VEC>(bb + c * Gs, b);
-                advance<VEC>(b, d, psi);
+        // descriptor windows A = [wb, wb+32), B = the next 32, as in the forward sweep
+        int64_t wb = beg;
+        int cA, cB;
+        float dA, dB;
+        decode(P, wb + lane, beg, end, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, cB, dB);
+        auto desc = [&](int64_t j, int &c, float &d) {
+            int k = (int)(j - wb);
+            if (k >= 32) {
+                cA = cB;
+                dA = dB;
+                wb += 32;
+                k -= 32;
+                decode(P, wb + 32 + lane, beg, end, cB, dB);
             }
+            c = __shfl_sync(FULL, cA, k);
+            d = __shfl_sync(FULL, dA, k);
+        };
+        int c0 = -1;
+        float d0 = 0.0f;
+        float4 b0[VEC];
+        if (beg < end) {
+            desc(beg, c0, d0);
+            if (c0 >= 0 && act) load4<VEC>(bb + c0 * Gs, b0);
+        }
+        for (int64_t j = beg; j < end; j++) {
+            int c1 = -1;
+            float d1 = 0.0f;
+            float4 b1[VEC];
+            if (j + 1 < end) {
+                desc(j + 1, c1, d1);
+                if (c1 >= 0 && act) load4<VEC>(bb + c1 * Gs, b1);
+            }
+            if (act) {
+                st_psi<VEC>(A.hist + j * Gs + g0, psi, nvalid);
+                if (c0 >= 0) advance<VEC>(b0, d0, psi);
+            }
+            c0 = c1;
+            d0 = d1;
+#pragma unroll
+            for (int v = 0; v < VEC; v++) b0[v] = b1[v];
         }
     }
 }
@@ -193,25 +228,43 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
         const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
         Vec<VEC> lam;
         if (act) lam = ld_psi<VEC>(A.v + (int64_t)t * Gs + g0, nvalid);
-        // windows from the end: lane l holds segment we - 32 + l
-        for (int64_t we = end; we > beg; we -= 32) {
-            int cw;
-            float dw;
-            decode(P, we - 32 + lane, beg, end, cw, dw);
-            const int n = we - beg < 32 ? (int)(we - beg) : 32;
-            for (int k = 31; k >= 32 - n; k--) {
-                const int c = __shfl_sync(FULL, cw, k);
-                const float d = __shfl_sync(FULL, dw, k);
-                if (!act || c < 0) continue;
-                const int64_t j = we - 32 + k;
-                float4 b[VEC];
-                load4<VEC>(bb + c * Gs, b);
-                const Vec<VEC> psi = ld_psi<VEC>(A.hist + j * Gs + g0, nvalid);
-                const Vec<VEC> wv = ld_psi<VEC>(A.w + c * Gs + g0, nvalid);
+        // descriptor windows from the end: A = [wa, wa+32), B = the 32 before it
+        int64_t wa = end - 32;
+        int cA, cB;
+        float dA, dB;
+        decode(P, wa + lane, beg, end, cA, dA);
+        decode(P, wa - 32 + lane, beg, end, cB, dB);
+        auto fetch = [&](int64_t j, RevSeg<VEC> &sg) {
+            int k = (int)(j - wa);
+            if (k < 0) {
+                cA = cB;
+                dA = dB;
+                wa -= 32;
+                k += 32;
+                decode(P, wa - 32 + lane, beg, end, cB, dB);
+            }
+            sg.c = __shfl_sync(FULL, cA, k);
+            sg.d = __shfl_sync(FULL, dA, k);
+            if (sg.c >= 0 && act) {
+                load4<VEC>(bb + sg.c * Gs, sg.b);
+                sg.psi = ld_psi<VEC>(A.hist + j * Gs + g0, nvalid);
+                sg.w = ld_psi<VEC>(A.w + sg.c * Gs + g0, nvalid);
+            }
+        };
+        RevSeg<VEC> cur, nxt;
+        cur.c = -1;
+        if (end > beg) fetch(end - 1, cur);
+        for (int64_t j = end - 1; j >= beg; j--) {
+            nxt.c = -1;
+            if (j - 1 >= beg) fetch(j - 1, nxt);
+            const int c = cur.c;
+            if (act && c >= 0) {
+                const float d = cur.d;
 #pragma unroll
                 for (int q = 0; q < VEC; q++) {
-                    const float s = b[q].x, a0 = b[q].y, a1 = b[q].z, a2 = b[q].w;
-                    const float ps = psi.v[q], la = lam.v[q], W = P.weight * wv.v[q];
+                    const float s = cur.b[q].x, a0 = cur.b[q].y, a1 = cur.b[q].z,
+                                a2 = cur.b[q].w;
+                    const float ps = cur.psi.v[q], la = lam.v[q], W = P.weight * cur.w.v[q];
                     const float tau = s * d;
                     const AdjTerms x = adj_terms(tau);
                     const float rs = rcp_approx(s), rs2 = rs * rs, rs3 = rs2 * rs;
@@ -237,6 +290,7 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
                     }
                 }
             }
+            cur = nxt;
         }
         if (act) st_psi<VEC>(A.dpsi_in + (int64_t)t * Gs + g0, lam, nvalid);
     }

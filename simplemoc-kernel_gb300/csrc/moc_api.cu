@@ -729,7 +729,13 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     sp.weight = o->weight;
     sp.err = h->err;
     sp.counter = h->counter;
-    const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
+    // The reverse sweep carries more work per segment than the forward: with few tracks
+    // (fewer warps than about two per SM slot) split the groups finer for parallelism.
+    int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
+    while (!o->vec && vec > 1 &&
+           (int64_t)p->n_tracks * ((p->n_groups + 32 * vec - 1) / (32 * vec)) <
+               (int64_t)h->sm_count * 64)
+        vec /= 2;
     sp.n_chunks = (p->n_groups + 32 * vec - 1) / (32 * vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
     ap.hist = h->hist;

@@ -292,11 +292,15 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         }
     } else {
         // RD - 1 segments ahead, through a per-warp ring in shared memory filled by
-        // cp.async: ring[(slot * VEC + v) * 32 + lane] holds group g0 + v of the segment
-        // in that slot. Each lane reads only what it copied, so the wait on its own copy
-        // groups is the only synchronisation. The issue pointer runs RD - 1 segments
-        // ahead of the compute pointer, inside descriptor windows A and B.
+        // cp.async: slot s holds the warp's 32*VEC consecutive cell-block entries of the
+        // segment in it, copied coalesced (lane l copies entries l, l+32, ...), so every
+        // 32-byte L2 sector is fetched once; lane l then reads its VEC entries
+        // (l*VEC ... l*VEC+VEC-1) after the wait on its copy groups and a __syncwarp.
+        // The issue pointer runs RD - 1 segments ahead of the compute pointer, inside
+        // descriptor windows A and B.
         static_assert(ST == STORE_F32 && (RD & (RD - 1)) == 0 && RD <= 16, "ring");
+        const int gw = g0 - lane * VEC;                   // first group of the warp's chunk
+        const int nrow = Gs - gw < 32 * VEC ? Gs - gw : 32 * VEC;  // entries inside the row
         auto peek = [&](int64_t jj, int &c, float &d) {
             const int k = (int)(jj - wb);
             if (k < 32) {
@@ -307,16 +311,18 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
                 d = __shfl_sync(FULL, dB, k - 32);
             }
         };
-        const float4 *blk = static_cast<const float4 *>(P.blk) + g0;
+        const float4 *blk = static_cast<const float4 *>(P.blk) + gw;
         auto issue = [&](int64_t jj, int slot) {
             if (jj < end) {
                 int c;
                 float d;
                 peek(jj, c, d);
-                if (c >= 0 && act) {
+                if (c >= 0) {
 #pragma unroll
-                    for (int v = 0; v < VEC; v++)
-                        cp_async16(ring + (slot * VEC + v) * 32 + lane, blk + c * Gs + v);
+                    for (int v = 0; v < VEC; v++) {
+                        const int q = v * 32 + lane;
+                        if (q < nrow) cp_async16(ring + slot * VEC * 32 + q, blk + c * Gs + q);
+                    }
                 }
             }
             cp_async_commit();
@@ -333,17 +339,20 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
             const int slot = (int)((j - beg) & (RD - 1));
             issue(j + RD - 1, (slot + RD - 1) & (RD - 1));
             cp_async_wait<RD - 1>();
+            __syncwarp();
             int c;
             float d;
             peek(j, c, d);
             if (c >= 0 && act) {
                 Blk<VEC> b;
 #pragma unroll
-                for (int v = 0; v < VEC; v++) b.v[v] = ring[(slot * VEC + v) * 32 + lane];
+                for (int v = 0; v < VEC; v++) b.v[v] = ring[slot * VEC * 32 + lane * VEC + v];
                 step(b, c, d);
             }
+            __syncwarp();  // the slot is refilled by the next iteration's copies
         }
         cp_async_wait<0>();
+        __syncwarp();
     }
     if (act) st_psi<VEC>(psi_row, psi, nvalid);
 }
