@@ -237,7 +237,7 @@ def gpu_arm(args, workload):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    step_ms, sweep_ms, prep_ms = [], [], []
+    step_ms, sweep_ms, prep_ms, split_ms = [], [], [], []
     launches = 0
     for _ in range(args.steps):
         flush.zero_()
@@ -251,6 +251,7 @@ def gpu_arm(args, workload):
         step_ms.append(e0.elapsed_time(e1))
         sweep_ms.append(t.sweep_ms)
         prep_ms.append(t.prep_ms)
+        split_ms.append(t.split_ms)
         launches += t.launches
     torch.cuda.synchronize(dev)
     if ws > 1:
@@ -299,7 +300,8 @@ def gpu_arm(args, workload):
             "achieved": l2_bytes / sweep_s / 1e9,
             "algorithmic_bytes_per_unit": per["gather"] + per["reduce"],
             "units_per_launch": units, "sweep_ms": sweep_s * 1e3,
-            "prep_ms": statistics.mean(prep_ms), "traffic": None}
+            "prep_ms": statistics.mean(prep_ms), "split_ms": statistics.mean(split_ms),
+            "traffic": None}
     terms = {}
     if "l2_mix_gbs" in peaks:
         # every resource the sweep needs, at its measured peak; the largest time binds
@@ -352,13 +354,14 @@ def gpu_arm(args, workload):
 
 
 def _time_fwd(h, dp, opts, reps=3):
-    """Median device time of prep + sweep + finish over reps calls (after one warm-up)."""
+    """Median device time of prep + split passes + sweep + finish over reps calls (after
+    one warm-up)."""
     h.fwd(dp, opts)
     ts = []
     for _ in range(reps):
         h.fwd(dp, opts)
         t = h.timings()
-        ts.append(t.prep_ms + t.sweep_ms + t.finish_ms)
+        ts.append(t.prep_ms + t.split_ms + t.sweep_ms + t.finish_ms)
     if h.synchronize():
         raise RuntimeError("device error")
     return statistics.median(ts)

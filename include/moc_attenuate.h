@@ -45,7 +45,7 @@
 extern "C" {
 #endif
 
-#define MOC_ABI_VERSION 1
+#define MOC_ABI_VERSION 2
 
 typedef enum {
     MOC_OK = 0,
@@ -140,7 +140,13 @@ typedef struct {
                                      arithmetic: 0 = auto, 1 = one (registers), 8 = seven,
                                      through a cp.async ring in shared memory (plain and
                                      stable FP32 forms with FP32 tallies)                  */
-    int32_t reserved[2];
+    int32_t track_chunk;          /* long tracks sweep in parallel chunks: a track of more
+                                     than 4 * C segments is cut into chunks of C segments,
+                                     joined through the affine form of the psi recursion.
+                                     0 = auto (C = 256), -1 = never cut, else C in
+                                     32 .. 2^24. Where a track is cut depends only on its
+                                     length and C                                          */
+    int32_t reserved[1];
 } moc_fwd_opts_t;
 
 /* Device time of each kernel of the last call made with opts.profile = 1. */
@@ -149,6 +155,8 @@ typedef struct {
     float sweep_ms;               /* the sweep kernel                                    */
     float finish_ms;              /* tally finishing pass (0 when the form has none)     */
     int32_t launches;             /* kernels the call launched                           */
+    float split_ms;               /* long-track split passes (records, chunk maps, chunk
+                                     starts) of the forward sweep; 0 when none ran        */
 } moc_timings_t;
 
 /* Reference defaults: FULL exp, N=353 / maxVal=10 table, FP32, atomic tallies,

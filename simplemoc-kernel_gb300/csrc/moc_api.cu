@@ -25,6 +25,15 @@ struct moc_handle_s {
     size_t gblk_cap = 0;
     float *hist = nullptr;     // adjoint: psi entering every segment
     size_t hist_cap = 0;
+    // long-track split: per-track record base, scan sums, records, starts and maps
+    int64_t *sbase = nullptr, *sbsum = nullptr;
+    size_t sbase_cap = 0, sbsum_cap = 0;
+    int4 *srec = nullptr;
+    size_t srec_cap = 0;
+    int64_t *smlist = nullptr;   // map list; smlist[cap] holds the map count
+    size_t smlist_cap = 0;
+    float *sstart = nullptr, *smap = nullptr;
+    size_t sstart_cap = 0, smap_cap = 0;
     // batching form
     float4 *bblk = nullptr;    // cell blocks of all problems of a batch
     size_t bblk_cap = 0;
@@ -50,9 +59,10 @@ struct moc_handle_s {
     size_t hcap[8] = {};
     cudaStream_t hstream = nullptr;
     // kernel timing of the last profiled call
-    cudaEvent_t ev[4] = {};
+    cudaEvent_t ev[5] = {};   // start, after prep, after sweep, after finish, after split
     int timed_launches = 0;   // 0: no profiled call yet
     bool timed_finish = false;
+    bool timed_split = false;
     std::string last_error;
 };
 
@@ -108,6 +118,9 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
     if (o->vec != 0 && o->vec != 1 && o->vec != 2 && o->vec != 4) return MOC_ERR_INVALID_ARG;
     if (o->warps_per_block < 0 || o->warps_per_block > 8) return MOC_ERR_INVALID_ARG;
     if (o->prefetch != 0 && o->prefetch != 1 && o->prefetch != moc::RING_DEPTH)
+        return MOC_ERR_INVALID_ARG;
+    if (o->track_chunk != 0 && o->track_chunk != -1 &&
+        (o->track_chunk < 32 || o->track_chunk > moc::SPLIT_CHUNK_MAX))
         return MOC_ERR_INVALID_ARG;
     if (o->prefetch == moc::RING_DEPTH &&
         (o->precision == MOC_PREC_BF16 || o->precision == MOC_PREC_FP16 ||
@@ -255,6 +268,56 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
         sp.ff64 = h->ff64;
     }
 
+    // Long tracks: chunk records, the maps of non-last chunks, the chunk starts.
+    const int chunk = o->track_chunk == 0 ? moc::SPLIT_CHUNK_DEFAULT : o->track_chunk;
+    // (record and map counts share one 64-bit scan: both must stay below 2^31)
+    const bool split = o->track_chunk != -1 &&
+                       p->n_segments > (int64_t)moc::SPLIT_MIN_FACTOR * chunk &&
+                       moc::split_max_records(p->n_tracks, p->n_segments, chunk) < INT32_MAX;
+    moc::SplitWork sw{};
+    moc::FwdConfig mcfg = cfg;
+    if (split) {
+        const int64_t T = p->n_tracks, Gs = p->group_stride;
+        const int64_t cap = moc::split_max_records(T, p->n_segments, chunk);
+        const int64_t nb = (T + 1023) / 1024;
+        if ((s = ensure(h, reinterpret_cast<void **>(&h->sbase), &h->sbase_cap,
+                        (size_t)(T + 1) * sizeof(int64_t))) ||
+            (s = ensure(h, reinterpret_cast<void **>(&h->sbsum), &h->sbsum_cap,
+                        (size_t)nb * sizeof(int64_t))) ||
+            (s = ensure(h, reinterpret_cast<void **>(&h->srec), &h->srec_cap,
+                        (size_t)cap * sizeof(int4))) ||
+            (s = ensure(h, reinterpret_cast<void **>(&h->smlist), &h->smlist_cap,
+                        (size_t)(cap + 1) * sizeof(int64_t))) ||
+            (s = ensure(h, reinterpret_cast<void **>(&h->sstart), &h->sstart_cap,
+                        (size_t)cap * Gs * sizeof(float))) ||
+            (s = ensure(h, reinterpret_cast<void **>(&h->smap), &h->smap_cap,
+                        2 * (size_t)cap * Gs * sizeof(float))))
+            return s;
+        sw.base = h->sbase;
+        sw.bsum = h->sbsum;
+        sw.rec = h->srec;
+        sw.map_list = h->smlist;
+        sw.n_map = h->smlist + cap;
+        sw.cap = cap;
+        sw.chunk = chunk;
+        sp.rec = h->srec;
+        sp.n_rec = h->sbase + T;
+        sp.map_list = sw.map_list;
+        sp.n_map = sw.n_map;
+        sp.rec_cap = cap;
+        sp.start = h->sstart;
+        sp.map_a = h->smap;
+        sp.map_b = h->smap + cap * Gs;
+        mcfg.mode = 1;
+        mcfg.prefetch = (cfg.prefetch == moc::RING_DEPTH && cfg.store == moc::STORE_F32)
+                            ? moc::RING_DEPTH
+                            : 1;
+        mcfg.tally = moc::TALLY_F32;
+        const int per_sm = moc::fwd_blocks_per_sm(mcfg, o->table_points);
+        if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+        mcfg.blocks = per_sm * h->sm_count;
+    }
+
     const bool prof = o->profile != 0;
     if (prof && !h->ev[0])
         for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
@@ -269,16 +332,26 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
                                              o->dz, o->zin, o->mu, o->mu2, st));
     if (sp.lo) MOC_CUDA(h, cudaMemsetAsync(sp.lo, 0, nff * sizeof(float), st));
     if (sp.ff64) MOC_CUDA(h, cudaMemsetAsync(sp.ff64, 0, nff * sizeof(double), st));
-    MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), st));
+    // counter[0]: the sweep's queue head, counter[1]: the map pass's
+    MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, 2 * sizeof(unsigned long long), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
+    if (split) {
+        MOC_CUDA(h, moc::launch_split_records(sp, sw, st));
+        moc::SweepParams mp = sp;
+        mp.counter = h->counter + 1;
+        MOC_CUDA(h, moc::launch_fwd(mp, mcfg, st));
+        MOC_CUDA(h, moc::launch_split_start(sp, sw, st));
+    }
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[4], st));
     MOC_CUDA(h, moc::launch_fwd(sp, cfg, st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
     const bool finish = sp.lo || sp.ff64;
     if (finish) MOC_CUDA(h, moc::launch_finish(p->fine_flux, sp.lo, sp.ff64, (int64_t)nff, st));
     if (prof) {
         if (finish) MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
-        h->timed_launches = finish ? 3 : 2;
+        h->timed_launches = (finish ? 3 : 2) + (split ? 5 : 0);
         h->timed_finish = finish;
+        h->timed_split = split;
     }
     return MOC_OK;
 }
@@ -501,6 +574,12 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->ff64) cudaFree(h->ff64);
     if (h->gblk) cudaFree(h->gblk);
     if (h->hist) cudaFree(h->hist);
+    if (h->sbase) cudaFree(h->sbase);
+    if (h->sbsum) cudaFree(h->sbsum);
+    if (h->srec) cudaFree(h->srec);
+    if (h->smlist) cudaFree(h->smlist);
+    if (h->sstart) cudaFree(h->sstart);
+    if (h->smap) cudaFree(h->smap);
     if (h->bblk) cudaFree(h->bblk);
     if (h->bhist) cudaFree(h->bhist);
     if (h->bperm) cudaFree(h->bperm);
@@ -589,6 +668,7 @@ moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs,
         MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
         h->timed_launches = n + (B.n_items ? 7 : 0);
         h->timed_finish = false;
+        h->timed_split = false;
     }
     return MOC_OK;
 }
@@ -787,6 +867,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
         MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
         h->timed_launches = launches + 1;
         h->timed_finish = true;
+        h->timed_split = false;
     }
     return MOC_OK;
 }
@@ -871,14 +952,20 @@ moc_status_t moc_last_timings(moc_handle_t h, moc_timings_t *t)
     if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
     const cudaEvent_t last = h->timed_finish ? h->ev[3] : h->ev[2];
     MOC_CUDA(h, cudaEventSynchronize(last));
-    float a = 0, b = 0, c = 0;
+    float a = 0, b = 0, c = 0, d = 0;
     MOC_CUDA(h, cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
-    MOC_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
+    if (h->timed_split) {
+        MOC_CUDA(h, cudaEventElapsedTime(&d, h->ev[1], h->ev[4]));
+        MOC_CUDA(h, cudaEventElapsedTime(&b, h->ev[4], h->ev[2]));
+    } else {
+        MOC_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
+    }
     if (h->timed_finish) MOC_CUDA(h, cudaEventElapsedTime(&c, h->ev[2], h->ev[3]));
     t->prep_ms = a;
     t->sweep_ms = b;
     t->finish_ms = c;
     t->launches = h->timed_launches;
+    t->split_ms = d;
     return MOC_OK;
 }
 

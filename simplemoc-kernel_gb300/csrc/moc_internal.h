@@ -40,6 +40,17 @@ enum TallyKind : int {
     TALLY_F64 = 2,   // red.global.add.f64 into a double accumulator
 };
 
+// Long tracks are cut into chunks that sweep in parallel (moc_split.cu). A chunk record
+// is an int4 {beg (low 32 bits), beg (high 32 bits), len | flags, track}.
+enum : int32_t {
+    CHUNK_LEN_MASK = 0x0fffffff,
+    CHUNK_SINGLE = 1 << 30,  // the whole track: psi read and written in place
+    CHUNK_LAST = 1 << 29,    // a split track's last chunk: writes the track's psi
+};
+constexpr int SPLIT_CHUNK_DEFAULT = 256;  // chunk length of split tracks
+constexpr int SPLIT_MIN_FACTOR = 4;       // tracks longer than 4 chunks are split
+constexpr int SPLIT_CHUNK_MAX = 1 << 24;
+
 // Everything a sweep launch reads. Device pointers.
 struct SweepParams {
     int32_t R, I, G, Gs, T, n_chunks;
@@ -60,7 +71,34 @@ struct SweepParams {
     float tab_dx, tab_max;
     int32_t *err;
     unsigned long long *counter;  // work-queue head, zeroed before each launch
+    // split mode (rec != null): work items are (chunk record, group chunk)
+    const int4 *rec;              // chunk records, in track order
+    const int64_t *n_rec;         // number of records (device)
+    const int64_t *map_list;      // record ids of the non-last chunks (map items)
+    const int64_t *n_map;         // their number (device)
+    int64_t rec_cap;              // records the buffers hold (items beyond are not run)
+    float *start;                 // [records][Gs] psi entering each chunk of a split track
+    float *map_a, *map_b;         // [records][Gs] psi_out = a psi_in + b of non-last chunks
 };
+
+// Split workspace (device) and the chunk length.
+struct SplitWork {
+    int64_t *base;    // [T + 1] first record of each track; base[T] = records
+    int64_t *bsum;    // [ceil(T / 1024)] scan block sums
+    int4 *rec;        // [cap]
+    int64_t *map_list;  // [cap] record ids of non-last chunks
+    int64_t *n_map;     // number of map items
+    int64_t cap;      // split_max_records(); offsets that are not a partition of [0, S]
+                      // can ask for more: those records are dropped and reported
+    int32_t chunk;
+};
+// Upper bound on the records of a problem (tracks + S / chunk).
+int64_t split_max_records(int64_t T, int64_t S, int chunk);
+// Records of every track (scan of the chunk counts, then the records; 3 launches).
+cudaError_t launch_split_records(const SweepParams &P, const SplitWork &W, cudaStream_t st);
+// psi entering every chunk of the split tracks from the maps: start_0 = psi_in,
+// start_{k+1} = a_k start_k + b_k.
+cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStream_t st);
 
 // Cell blocks of every (region, interval) and group: blk[c][g] = (sigT of the region,
 // q0, q1*mu, q2*mu2), the coefficients rounded exactly as src/cpu/kernel.c:111-191 and
@@ -86,6 +124,7 @@ struct FwdConfig {
     int store = STORE_F32;
     int tally = TALLY_F32;
     int prefetch = 1;     // 1: registers, one segment ahead; RING_DEPTH: cp.async ring
+    int mode = 0;         // 0: the sweep; 1: affine maps of split chunks (split mode)
 };
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &cfg, cudaStream_t st);
 // Dynamic shared memory of a configuration (table of tab_n pairs in table mode + rings).

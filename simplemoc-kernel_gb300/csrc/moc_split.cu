@@ -1,0 +1,205 @@
+// moc_split.cu — long tracks cut into chunks that sweep in parallel.
+//
+// psi is carried along a track segment by segment (src/cpu/kernel.c:53, 289-331): per
+// group psi' = p psi + b, with p = exp(-tau) and b the source part of the attenuated
+// flux, which does not depend on psi. A run of segments is therefore the affine map
+// psi_out = a psi_in + b, with a the product of the p's and b the sweep of the run from
+// psi = 0. A track of more than SPLIT_MIN_FACTOR * C segments is cut into chunks of C
+// segments (the last one shorter):
+//   1. records: an exclusive scan of the chunk counts of the tracks, one record per chunk;
+//   2. maps: the sweep kernel in map mode composes (a, b) of every non-last chunk;
+//   3. starts: per track and group, psi entering each chunk, start_0 = psi_in,
+//      start_{k+1} = a_k start_k + b_k;
+//   4. the sweep runs every chunk from its start, with tallies, all chunks at once; a
+//      split track's last chunk writes the track's outgoing psi.
+// Whether and where a track is cut depends on its length only, so a track's psi is the
+// same whatever the other tracks of the problem are. Shorter tracks are one record and
+// sweep exactly as in one pass.
+#include "moc_internal.h"
+
+namespace moc {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int SCAN_BLOCK = 1024;
+
+__device__ __forceinline__ bool track_ok(int64_t a, int64_t b, int64_t S)
+{
+    return a >= 0 && a <= b && b <= S;
+}
+
+__device__ __forceinline__ int64_t chunks_of(int64_t len, int64_t C)
+{
+    return len > SPLIT_MIN_FACTOR * C ? (len + C - 1) / C : 1;
+}
+
+// Records of track t (1 for a track with bad offsets: it is reported and skipped).
+__device__ __forceinline__ int64_t count_of(const SweepParams &P, const SplitWork &W, int64_t t)
+{
+    const int64_t a = P.off[t], b = P.off[t + 1];
+    const int64_t n = track_ok(a, b, P.S) ? chunks_of(b - a, W.chunk) : 1;
+    return n < W.cap ? n : W.cap;
+}
+
+// Records and map items (non-last chunks) of a track, packed for one scan: maps in the
+// high 32 bits, records in the low 32 (both totals stay below 2^32: the host caps them).
+__device__ __forceinline__ int64_t packed_count(int64_t n)
+{
+    return ((n > 1 ? n - 1 : 0) << 32) | n;
+}
+
+// Inclusive scan of v over the block; *total = the block's sum. Called by every thread.
+__device__ int64_t block_incl_scan(int64_t v, int64_t *total)
+{
+    __shared__ int64_t ws[SCAN_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t u = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) ws[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int64_t s = lane < nw ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t u = __shfl_up_sync(FULL, s, o);
+            if (lane >= o) s += u;
+        }
+        if (lane < nw) ws[lane] = s;
+    }
+    __syncthreads();
+    if (w > 0) v += ws[w - 1];
+    *total = ws[nw - 1];
+    __syncthreads();  // ws is reused by the next call
+    return v;
+}
+
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_sums_kernel(const SweepParams P,
+                                                               const SplitWork W)
+{
+    const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
+    int64_t total;
+    block_incl_scan(t < P.T ? packed_count(count_of(P, W, t)) : 0, &total);
+    if (threadIdx.x == 0) W.bsum[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of the nb block sums, in place.
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_bsum_kernel(int64_t *bsum, int64_t nb)
+{
+    int64_t carry = 0;
+    for (int64_t b0 = 0; b0 < nb; b0 += SCAN_BLOCK) {
+        const int64_t i = b0 + threadIdx.x;
+        const int64_t v = i < nb ? bsum[i] : 0;
+        int64_t total;
+        const int64_t incl = block_incl_scan(v, &total);
+        if (i < nb) bsum[i] = carry + incl - v;
+        carry += total;
+    }
+}
+
+// base[t] = exclusive prefix of the record counts; thread t then writes track t's
+// records and the ids of its non-last chunks into the map list.
+__global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepParams P,
+                                                                   const SplitWork W)
+{
+    const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
+    const int64_t n = t < P.T ? count_of(P, W, t) : 0;
+    const int64_t pk = packed_count(n);
+    int64_t total;
+    const int64_t incl = block_incl_scan(pk, &total);
+    if (t >= P.T) return;
+    const int64_t excl = W.bsum[blockIdx.x] + incl - pk;
+    const int64_t b = excl & 0xffffffffLL, mb = excl >> 32;
+    W.base[t] = b;
+    if (t == P.T - 1) {
+        W.base[P.T] = b + n;
+        *W.n_map = mb + (n > 1 ? n - 1 : 0);
+    }
+    for (int64_t k = 0; k + 1 < n; k++)
+        if (b + k < W.cap && mb + k < W.cap) W.map_list[mb + k] = b + k;
+    const int64_t a = P.off[t], e = P.off[t + 1];
+    bool dropped = false;
+    auto put = [&](int64_t q, int64_t beg, int64_t len, int32_t flags) {
+        if (q >= W.cap) {  // overlapping offsets: more chunks than S allows
+            dropped = true;
+            return;
+        }
+        W.rec[q] = make_int4((int32_t)(uint32_t)(uint64_t)beg, (int32_t)(beg >> 32),
+                             (int32_t)len | flags, (int32_t)t);
+    };
+    if (!track_ok(a, e, P.S)) {
+        atomicOr(P.err, DEVERR_OFFSETS);
+        put(b, 0, 0, CHUNK_SINGLE);  // psi passes through unchanged
+        return;
+    }
+    if (n == 1) {
+        put(b, a, e - a, CHUNK_SINGLE);
+    } else {
+        const int64_t C = W.chunk;
+        for (int64_t k = 0; k < n; k++) {
+            const int64_t beg = a + k * C;
+            const int64_t len = k + 1 < n ? C : e - beg;
+            put(b + k, beg, len, k + 1 < n ? 0 : CHUNK_LAST);
+        }
+    }
+    if (dropped) atomicOr(P.err, DEVERR_OFFSETS);
+}
+
+// psi entering each chunk of every split track: one warp per track, lanes over groups.
+__global__ void split_start_kernel(const SweepParams P, const SplitWork W)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < P.T;
+         t += nwarps) {
+        const int64_t b = W.base[t];
+        if (b >= W.cap) continue;
+        const int64_t e = W.base[t + 1] < W.cap ? W.base[t + 1] : W.cap;
+        const int64_t nq = e - b;
+        if (nq < 2) continue;
+        const float *__restrict__ ma = P.map_a;
+        const float *__restrict__ mb = P.map_b;
+        float *__restrict__ start = P.start;
+        for (int g = lane; g < P.G; g += 32) {
+            float psi = P.psi[t * P.Gs + g];
+            for (int64_t c = 0; c < nq; c++) {
+                const int64_t row = (b + c) * P.Gs + g;
+                start[row] = psi;
+                if (c + 1 < nq) psi = fmaf(ma[row], psi, mb[row]);
+            }
+        }
+    }
+}
+
+int grid_for(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+int64_t split_max_records(int64_t T, int64_t S, int chunk)
+{
+    return T + S / chunk + 1;
+}
+
+cudaError_t launch_split_records(const SweepParams &P, const SplitWork &W, cudaStream_t st)
+{
+    if (P.T < 1 || W.chunk < 1) return cudaErrorInvalidValue;
+    const int64_t nb = (P.T + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    scan_sums_kernel<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(P, W);
+    scan_bsum_kernel<<<1, SCAN_BLOCK, 0, st>>>(W.bsum, nb);
+    split_records_kernel<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(P, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStream_t st)
+{
+    split_start_kernel<<<grid_for((int64_t)P.T * 32), 256, 0, st>>>(P, W);
+    return cudaGetLastError();
+}
+
+}  // namespace moc

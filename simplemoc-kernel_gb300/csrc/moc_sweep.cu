@@ -153,10 +153,11 @@ struct TableRef {
 
 // src/cpu/kernel.c:200-332 for VEC groups. Divisions by sigT powers become products with
 // one reciprocal.
+// pmul gets p = exp(-tau) per group (the map mode's product; unused otherwise).
 template <int VEC, int EK>
 __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float weight,
                                           const TableRef &tr, Vec<VEC> &psi,
-                                          Vec<VEC> &tally)
+                                          Vec<VEC> &tally, Vec<VEC> &pmul)
 {
 #pragma unroll
     for (int k = 0; k < VEC; k++) {
@@ -195,6 +196,7 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
         float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);
         psi.v[k] = fmaf(ps, p, pn);
+        pmul.v[k] = p;
     }
 }
 
@@ -216,24 +218,69 @@ __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t 
     }
 }
 
-template <int VEC, int EK, int ST, int TL, int RD>
+enum : int { MODE_SWEEP = 0, MODE_MAP = 1 };
+
+// One work item. Without chunk records an item is (track, group chunk). With records
+// (split mode) it is (record, group chunk): a whole track (psi in place), or a chunk of
+// a split track, which starts from its precomputed psi and, if it is the track's last,
+// writes the track's psi. MODE_MAP runs the non-last chunks of split tracks from psi = 0
+// without tallies and writes (a, b) = (product of p, outgoing psi) per group.
+template <int VEC, int EK, int ST, int TL, int RD, int MODE>
 __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int lane,
                                            const TableRef &tr, float4 *ring)
 {
-    const int t = (int)(item / P.n_chunks);
-    const int ch = (int)(item - (int64_t)t * P.n_chunks);
+    const int Gs = P.Gs;
+    int64_t beg, end, row_q = 0;
+    int ch;
+    const float *psi_in;
+    float *psi_out;  // null: the chunk's outgoing psi is not kept
+    if (P.rec) {
+        int64_t q = item / P.n_chunks;
+        ch = (int)(item - q * P.n_chunks);
+        if constexpr (MODE == MODE_MAP) {
+            q = P.map_list[q];
+            if ((uint64_t)q >= (uint64_t)P.rec_cap) return;
+        }
+        const int4 r = __ldg(P.rec + q);
+        const int flags = r.z;
+        if constexpr (MODE == MODE_MAP)
+            if (flags & (CHUNK_SINGLE | CHUNK_LAST)) return;
+        beg = (int64_t)(uint32_t)r.x | ((int64_t)r.y << 32);
+        end = beg + (flags & CHUNK_LEN_MASK);
+        // records come from offsets that may not be a partition of [0, S]: check them
+        if (!(beg >= 0 && end <= P.S && (unsigned)r.w < (unsigned)P.T)) {
+            if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
+            return;
+        }
+        float *track_psi = P.psi + (int64_t)r.w * Gs;
+        if (flags & CHUNK_SINGLE) {
+            psi_in = psi_out = track_psi;
+        } else {
+            psi_in = P.start + q * Gs;
+            psi_out = (flags & CHUNK_LAST) ? track_psi : nullptr;
+        }
+        row_q = q * Gs;
+    } else {
+        const int t = (int)(item / P.n_chunks);
+        ch = (int)(item - (int64_t)t * P.n_chunks);
+        beg = P.off[t];
+        end = P.off[t + 1];
+        if (!(beg >= 0 && beg <= end && end <= P.S)) {
+            if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
+            return;
+        }
+        psi_in = psi_out = P.psi + (int64_t)t * Gs;
+    }
     const int g0 = (ch * 32 + lane) * VEC;
     const int nvalid = P.G - g0;
     const bool act = nvalid > 0;
-    const int64_t beg = P.off[t], end = P.off[t + 1];
-    if (!(beg >= 0 && beg <= end && end <= P.S)) {
-        if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
-        return;
+    Vec<VEC> psi, amul;
+#pragma unroll
+    for (int k = 0; k < VEC; k++) {
+        psi.v[k] = 0.0f;
+        amul.v[k] = 1.0f;
     }
-    const int Gs = P.Gs;
-    float *psi_row = P.psi + (int64_t)t * Gs + g0;
-    Vec<VEC> psi;
-    if (act) psi = ld_psi<VEC>(psi_row, nvalid);
+    if (MODE == MODE_SWEEP && act) psi = ld_psi<VEC>(psi_in + g0, nvalid);
 
     // Descriptor windows: A = segments [wb, wb+32), B = the next 32.
     int64_t wb = beg;
@@ -255,10 +302,13 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
     };
     auto step = [&](const Blk<VEC> &b, int c, float d) {
         if (c >= 0 && act) {
-            Vec<VEC> tally;
-            attenuate<VEC, EK>(b, d, P.weight, tr, psi, tally);
+            Vec<VEC> tally, p;
+            attenuate<VEC, EK>(b, d, P.weight, tr, psi, tally, p);
             const int idx = c * Gs + g0;
-            if constexpr (TL == TALLY_F32)
+            if constexpr (MODE == MODE_MAP) {
+#pragma unroll
+                for (int k = 0; k < VEC; k++) amul.v[k] *= p.v[k];
+            } else if constexpr (TL == TALLY_F32)
                 red_row<VEC>(P.ff + idx, tally, nvalid);
             else if constexpr (TL == TALLY_COMP)
                 comp_row<VEC>(P.ff + idx, P.lo + idx, tally, nvalid);
@@ -354,12 +404,18 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         cp_async_wait<0>();
         __syncwarp();
     }
-    if (act) st_psi<VEC>(psi_row, psi, nvalid);
+    if (!act) return;
+    if constexpr (MODE == MODE_MAP) {
+        st_psi<VEC>(P.map_a + row_q + g0, amul, nvalid);
+        st_psi<VEC>(P.map_b + row_q + g0, psi, nvalid);
+    } else {
+        if (psi_out) st_psi<VEC>(psi_out + g0, psi, nvalid);
+    }
 }
 
 // Dynamic shared memory: the exponential table (table mode), then one prefetch ring of
 // RD * VEC * 32 float4 per warp.
-template <int VEC, int EK, int ST, int TL, int RD>
+template <int VEC, int EK, int ST, int TL, int RD, int MODE>
 __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
 {
     extern __shared__ float4 s_dyn[];
@@ -377,12 +433,26 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD * VEC * 32);
     }
     const int lane = threadIdx.x & 31;
+    int64_t n_items = P.n_items;
+    if (P.rec) {
+        const int64_t n = MODE == MODE_MAP ? *P.n_map : *P.n_rec;
+        n_items = (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
+    }
+    if constexpr (MODE == MODE_MAP) {
+        // Map items (the non-last chunks, listed by the record pass) are full chunks of
+        // equal length: a static warp-strided assignment balances without a queue atomic.
+        const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+        for (int64_t item = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+             item < n_items; item += nw)
+            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, lane, tr, ring);
+        return;
+    }
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= (unsigned long long)P.n_items) break;
-        sweep_item<VEC, EK, ST, TL, RD>(P, (int64_t)item, lane, tr, ring);
+        if (item >= (unsigned long long)n_items) break;
+        sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, lane, tr, ring);
     }
 }
 
@@ -414,10 +484,10 @@ __global__ void finish_kernel(float *__restrict__ ff, const float *__restrict__ 
     }
 }
 
-template <int VEC, int EK, int ST, int TL, int RD = 0>
+template <int VEC, int EK, int ST, int TL, int RD = 0, int MODE = MODE_SWEEP>
 const void *fwd_fn()
 {
-    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD>);
+    return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD, MODE>);
 }
 
 // The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
@@ -427,6 +497,31 @@ const void *fwd_fn()
 template <int V>
 const void *pick_vec(const FwdConfig &c)
 {
+    if (c.mode == MODE_MAP) {  // maps: no tallies; FP32 storage may use the ring
+        if (c.prefetch == RING_DEPTH) {
+            if (c.store != STORE_F32) return nullptr;
+            if (c.exp_kind == EXPK_PLAIN)
+                return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
+            if (c.exp_kind == EXPK_TABLE)
+                return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
+            return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
+        }
+        if (c.prefetch != 1) return nullptr;
+        if (c.store == STORE_F32) {
+            if (c.exp_kind == EXPK_PLAIN)
+                return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, 0, MODE_MAP>();
+            if (c.exp_kind == EXPK_TABLE)
+                return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, 0, MODE_MAP>();
+            return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, 0, MODE_MAP>();
+        }
+        if (c.exp_kind != EXPK_STABLE) return nullptr;
+        if (c.store == STORE_BF16)
+            return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, 0, MODE_MAP>();
+        if (c.store == STORE_F16)
+            return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32, 0, MODE_MAP>();
+        return nullptr;
+    }
+    if (c.mode != MODE_SWEEP) return nullptr;
     if (c.prefetch > 1) {
         if (c.prefetch != RING_DEPTH || c.store != STORE_F32 || c.tally != TALLY_F32)
             return nullptr;

@@ -65,13 +65,13 @@ class MocFwdOpts(C.Structure):
         ("dz", C.c_float), ("zin", C.c_float), ("weight", C.c_float), ("mu", C.c_float),
         ("mu2", C.c_float), ("checked", C.c_int32), ("vec", C.c_int32),
         ("warps_per_block", C.c_int32), ("profile", C.c_int32),
-        ("prefetch", C.c_int32), ("reserved", C.c_int32 * 2),
+        ("prefetch", C.c_int32), ("track_chunk", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
 class MocTimings(C.Structure):
     _fields_ = [("prep_ms", C.c_float), ("sweep_ms", C.c_float), ("finish_ms", C.c_float),
-                ("launches", C.c_int32)]
+                ("launches", C.c_int32), ("split_ms", C.c_float)]
 
 
 class MocTuneResult(C.Structure):
@@ -293,6 +293,20 @@ class HostProblem:
                            self.seg_region[idx].copy(), self.seg_interval[idx].copy(),
                            self.seg_ds[idx].copy(), self.sigT, self.source,
                            np.zeros_like(self.fine_flux), self.psi[tracks].copy())
+
+    def with_lengths(self, lens) -> "HostProblem":
+        """The first sum(lens) segments regrouped into tracks of the given lengths (same
+        tables, zero tallies); track t takes psi row t mod T."""
+        lens = np.asarray(lens, np.int64)
+        off = np.zeros(len(lens) + 1, np.int64)
+        off[1:] = np.cumsum(lens)
+        S = int(off[-1])
+        assert S <= self.S, "not enough segments"
+        rows = np.arange(len(lens)) % max(self.T, 1)
+        return HostProblem(self.R, self.I, self.G, self.Gs, len(lens), S, off,
+                           self.seg_region[:S].copy(), self.seg_interval[:S].copy(),
+                           self.seg_ds[:S].copy(), self.sigT, self.source,
+                           np.zeros_like(self.fine_flux), self.psi[rows].copy())
 
 
 def _aligned_empty(shape, dtype, align=64):

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + [
     "-I" + INCLUDE, "-I" + CSRC,
 ]
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu", "moc_adjoint.cu",
-              "moc_batch.cu"]
+              "moc_batch.cu", "moc_split.cu"]
 
 LIB = os.path.join(BUILD, "libmocatt.so")
 SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")

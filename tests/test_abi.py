@@ -40,7 +40,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_library_loads_and_reports_version():
     L = mocatt.lib()
-    assert L.moc_abi_version() == 1
+    assert L.moc_abi_version() == 2
     assert L.moc_status_string(mocatt.MOC_ERR_BAD_INDEX).decode().startswith("segment")
     assert L.moc_status_string(999) == b"unknown status"
 
