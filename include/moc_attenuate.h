@@ -143,9 +143,12 @@ typedef struct {
     int32_t track_chunk;          /* long tracks sweep in parallel chunks: a track of more
                                      than 4 * C segments is cut into chunks of C segments,
                                      joined through the affine form of the psi recursion.
-                                     0 = auto (C = 256), -1 = never cut, else C in
-                                     32 .. 2^24. Where a track is cut depends only on its
-                                     length and C                                          */
+                                     -1 = never cut; C in 32 .. 2^24 = that C (a track's
+                                     psi then depends only on its own segments and C);
+                                     0 = auto: C from the problem's size, so that no
+                                     whole track takes more than about a quarter of the
+                                     sweep (a power of two, >= 32). The no-allocation
+                                     entry point never cuts tracks                         */
     int32_t reserved[1];
 } moc_fwd_opts_t;
 
@@ -194,7 +197,8 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *pr
  * Batching form: sweep several problems (different group counts, tracks of very uneven
  * length) in ONE persistent kernel launch. No single counterpart in the reference (its
  * run_kernel, src/cpu/kernel.c:3-73, sweeps one problem); each problem is swept exactly
- * as moc_attenuate_fwd would sweep it (plain form, either exp mode; opts is shared).
+ * as moc_attenuate_fwd with track_chunk = -1 would sweep it (plain form, either exp mode;
+ * opts is shared; tracks are not cut into chunks).
  * Tracks are bucket-sorted by length on the device and consumed longest first from one
  * work queue; problems whose G does not fill a warp are swept by sub-warps carrying
  * several tracks each. The first call for a given set of problems (pointers and sizes)

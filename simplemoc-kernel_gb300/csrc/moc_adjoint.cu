@@ -19,6 +19,12 @@
 // they come from their Taylor sums, like the forward's stable terms. The exponentials
 // are recomputed from tau in the reverse sweep instead of being stored; psi entering
 // each segment is recorded by a first forward pass (one float per segment and group).
+//
+// Long tracks are split into chunks as in the forward (moc_split.cu): lambda obeys
+// lambda_in = p lambda_out + W e/s, affine backwards with the same factor a = prod p as
+// psi forwards, so one map pass gives (a, b, c) per chunk, a scan over each track's
+// chunks gives psi entering and lambda leaving every chunk, and the recording and
+// reverse passes then run all chunks in parallel.
 #include "moc_device.cuh"
 #include "moc_internal.h"
 
@@ -121,19 +127,51 @@ __device__ __forceinline__ void load4(const float4 *p, float4 (&b)[VEC])
     for (int k = 0; k < VEC; k++) b[k] = __ldg(p + k);
 }
 
-__device__ __forceinline__ bool item_range(const SweepParams &P, int64_t item, int lane, int vec,
-                                           int &t, int &g0, int64_t &beg, int64_t &end)
+// Work item of an adjoint pass: (track, group chunk), or (chunk record, group chunk)
+// when long tracks are split; a record's chunk starts from its precomputed psi (forward)
+// or lambda (reverse).
+struct AdjItem {
+    int64_t beg, end, q;  // q: the record (split tracks) or -1
+    int t, g0, flags;
+};
+
+__device__ __forceinline__ bool adj_item(const SweepParams &P, int64_t item, int lane, int vec,
+                                         AdjItem &it)
 {
-    t = (int)(item / P.n_chunks);
-    const int ch = (int)(item - (int64_t)t * P.n_chunks);
-    g0 = (ch * 32 + lane) * vec;
-    beg = P.off[t];
-    end = P.off[t + 1];
-    if (!(beg >= 0 && beg <= end && end <= P.S)) {
+    const int64_t u = item / P.n_chunks;
+    const int ch = (int)(item - u * P.n_chunks);
+    it.g0 = (ch * 32 + lane) * vec;
+    if (P.rec) {
+        const int4 r = __ldg(P.rec + u);
+        it.q = u;
+        it.t = r.w;
+        it.flags = r.z;
+        it.beg = (int64_t)(uint32_t)r.x | ((int64_t)r.y << 32);
+        it.end = it.beg + (r.z & CHUNK_LEN_MASK);
+        if (!(it.beg >= 0 && it.end <= P.S && (unsigned)r.w < (unsigned)P.T)) {
+            if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
+            return false;
+        }
+        return true;
+    }
+    it.q = -1;
+    it.t = (int)u;
+    it.flags = CHUNK_SINGLE;
+    it.beg = P.off[u];
+    it.end = P.off[u + 1];
+    if (!(it.beg >= 0 && it.beg <= it.end && it.end <= P.S)) {
         if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
         return false;
     }
     return true;
+}
+
+// Items of a pass: tracks (or records) times group chunks.
+__device__ __forceinline__ int64_t adj_items(const SweepParams &P)
+{
+    if (!P.rec) return P.n_items;
+    const int64_t n = *P.n_rec;
+    return (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
 }
 
 // One segment's inputs for the reverse sweep, fetched one segment ahead.
@@ -150,20 +188,24 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
+    const int64_t n_items = adj_items(P);
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= (unsigned long long)P.n_items) break;
-        int t, g0;
-        int64_t beg, end;
-        if (!item_range(P, (int64_t)item, lane, VEC, t, g0, beg, end)) continue;
+        if (item >= (unsigned long long)n_items) break;
+        AdjItem it;
+        if (!adj_item(P, (int64_t)item, lane, VEC, it)) continue;
+        const int g0 = it.g0;
+        const int64_t beg = it.beg, end = it.end;
         const int nvalid = P.G - g0;
         const bool act = nvalid > 0;
         const int Gs = P.Gs;
         const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        const float *psi_src = (it.flags & CHUNK_SINGLE) ? P.psi + (int64_t)it.t * Gs
+                                                         : P.start + it.q * Gs;
         Vec<VEC> psi;
-        if (act) psi = ld_psi<VEC>(P.psi + (int64_t)t * Gs + g0, nvalid);
+        if (act) psi = ld_psi<VEC>(psi_src + g0, nvalid);
         // descriptor windows A = [wb, wb+32), B = the next 32, as in the forward sweep
         int64_t wb = beg;
         int cA, cB;
@@ -214,20 +256,24 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
+    const int64_t n_items = adj_items(P);
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= (unsigned long long)P.n_items) break;
-        int t, g0;
-        int64_t beg, end;
-        if (!item_range(P, (int64_t)item, lane, VEC, t, g0, beg, end)) continue;
+        if (item >= (unsigned long long)n_items) break;
+        AdjItem it;
+        if (!adj_item(P, (int64_t)item, lane, VEC, it)) continue;
+        const int g0 = it.g0;
+        const int64_t beg = it.beg, end = it.end;
         const int nvalid = P.G - g0;
         const bool act = nvalid > 0;
         const int Gs = P.Gs;
         const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        const bool single = (it.flags & CHUNK_SINGLE) != 0;
+        const float *lam_src = single ? A.v + (int64_t)it.t * Gs : A.lam_end + it.q * Gs;
         Vec<VEC> lam;
-        if (act) lam = ld_psi<VEC>(A.v + (int64_t)t * Gs + g0, nvalid);
+        if (act) lam = ld_psi<VEC>(lam_src + g0, nvalid);
         // descriptor windows from the end: A = [wa, wa+32), B = the 32 before it
         int64_t wa = end - 32;
         int cA, cB;
@@ -292,7 +338,151 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
             }
             cur = nxt;
         }
-        if (act) st_psi<VEC>(A.dpsi_in + (int64_t)t * Gs + g0, lam, nvalid);
+        if (act && (single || (it.flags & CHUNK_FIRST)))
+            st_psi<VEC>(A.dpsi_in + (int64_t)it.t * Gs + g0, lam, nvalid);
+    }
+}
+
+// Maps of every chunk of a split track, per group: psi_out = a psi_in + b (forward) and
+// lambda_in = a lambda_out + c (reverse), with a the product of the chunk's p and
+// c = sum_j (product of p before segment j) W_j e_j / s_j, the chunk's lambda sources
+// carried to its start. The arithmetic of psi is the recording pass's (advance).
+template <int VEC>
+__global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
+{
+    const SweepParams &P = A.fw;
+    const int lane = threadIdx.x & 31;
+    int64_t n_items = 0;
+    {
+        const int64_t n = *P.n_map;
+        n_items = (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
+    }
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(P.counter, 1ULL);
+        item = __shfl_sync(FULL, item, 0);
+        if (item >= (unsigned long long)n_items) break;
+        const int64_t m = (int64_t)item / P.n_chunks;
+        const int ch = (int)((int64_t)item - m * P.n_chunks);
+        const int64_t q = P.map_list[m];
+        if ((uint64_t)q >= (uint64_t)P.rec_cap) continue;
+        AdjItem it;
+        if (!adj_item(P, q * P.n_chunks + ch, lane, VEC, it)) continue;
+        const int g0 = it.g0;
+        const int64_t beg = it.beg, end = it.end;
+        const int nvalid = P.G - g0;
+        const bool act = nvalid > 0;
+        const int Gs = P.Gs;
+        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        Vec<VEC> ma, mb, mc;
+#pragma unroll
+        for (int k = 0; k < VEC; k++) {
+            ma.v[k] = 1.0f;
+            mb.v[k] = 0.0f;
+            mc.v[k] = 0.0f;
+        }
+        int64_t wb = beg;
+        int cA, cB;
+        float dA, dB;
+        decode(P, wb + lane, beg, end, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, cB, dB);
+        auto desc = [&](int64_t j, int &c, float &d) {
+            int k = (int)(j - wb);
+            if (k >= 32) {
+                cA = cB;
+                dA = dB;
+                wb += 32;
+                k -= 32;
+                decode(P, wb + 32 + lane, beg, end, cB, dB);
+            }
+            c = __shfl_sync(FULL, cA, k);
+            d = __shfl_sync(FULL, dA, k);
+        };
+        int c0 = -1;
+        float d0 = 0.0f;
+        float4 b0[VEC];
+        Vec<VEC> w0;
+        if (beg < end) {
+            desc(beg, c0, d0);
+            if (c0 >= 0 && act) {
+                load4<VEC>(bb + c0 * Gs, b0);
+                w0 = ld_psi<VEC>(A.w + c0 * Gs + g0, nvalid);
+            }
+        }
+        for (int64_t j = beg; j < end; j++) {
+            int c1 = -1;
+            float d1 = 0.0f;
+            float4 b1[VEC];
+            Vec<VEC> w1;
+            if (j + 1 < end) {
+                desc(j + 1, c1, d1);
+                if (c1 >= 0 && act) {
+                    load4<VEC>(bb + c1 * Gs, b1);
+                    w1 = ld_psi<VEC>(A.w + c1 * Gs + g0, nvalid);
+                }
+            }
+            if (act && c0 >= 0) {
+#pragma unroll
+                for (int k = 0; k < VEC; k++) {
+                    const float s = b0[k].x, a0 = b0[k].y, a1 = b0[k].z, a2 = b0[k].w;
+                    const float tau = s * d0;
+                    const ExpTerms x = exp_terms_stable(tau);
+                    const float rs = rcp_approx(s), rs2 = rs * rs;
+                    const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * (rs * rs2));
+                    float pn = a0 * x.e * rs;
+                    pn = fmaf(a1 * x.tme, rs2, pn);
+                    pn = fmaf(a2, reuse, pn);
+                    mc.v[k] = fmaf(ma.v[k], P.weight * w0.v[k] * x.e * rs, mc.v[k]);
+                    mb.v[k] = fmaf(mb.v[k], x.p, pn);
+                    ma.v[k] *= x.p;
+                }
+            }
+            c0 = c1;
+            d0 = d1;
+#pragma unroll
+            for (int v = 0; v < VEC; v++) b0[v] = b1[v];
+            w0 = w1;
+        }
+        if (act) {
+            st_psi<VEC>(P.map_a + q * Gs + g0, ma, nvalid);
+            st_psi<VEC>(P.map_b + q * Gs + g0, mb, nvalid);
+            st_psi<VEC>(A.map_c + q * Gs + g0, mc, nvalid);
+        }
+    }
+}
+
+// psi entering and lambda leaving every chunk of the split tracks: one warp per track,
+// lanes over groups. psi_0 = psi_in, psi_{k+1} = a_k psi_k + b_k; lambda leaving the last
+// chunk = dL/dpsi_out, lambda leaving chunk k-1 = a_k lambda_k + c_k.
+__global__ void adj_start_kernel(const AdjParams A)
+{
+    const SweepParams &P = A.fw;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float *__restrict__ ma = P.map_a;
+    const float *__restrict__ mb = P.map_b;
+    const float *__restrict__ mc = A.map_c;
+    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < P.T;
+         t += nwarps) {
+        const int64_t b = A.base[t];
+        if (b >= P.rec_cap) continue;
+        const int64_t e = A.base[t + 1] < P.rec_cap ? A.base[t + 1] : P.rec_cap;
+        const int64_t nq = e - b;
+        if (nq < 2) continue;
+        for (int g = lane; g < P.G; g += 32) {
+            float psi = P.psi[t * P.Gs + g];
+            for (int64_t k = 0; k < nq; k++) {
+                const int64_t row = (b + k) * P.Gs + g;
+                P.start[row] = psi;
+                psi = fmaf(ma[row], psi, mb[row]);
+            }
+            float lam = A.v[t * P.Gs + g];
+            for (int64_t k = nq - 1; k >= 0; k--) {
+                const int64_t row = (b + k) * P.Gs + g;
+                A.lam_end[row] = lam;
+                lam = fmaf(ma[row], lam, mc[row]);
+            }
+        }
     }
 }
 
@@ -372,6 +562,37 @@ cudaError_t launch_adj_forward(const AdjParams &p, int vec, int blocks, cudaStre
 cudaError_t launch_adj_reverse(const AdjParams &p, int vec, int blocks, cudaStream_t st)
 {
     return launch(p, vec, blocks, true, st);
+}
+
+int adj_map_blocks_per_sm(int vec)
+{
+    const void *fn = vec == 1   ? reinterpret_cast<const void *>(&adj_map_kernel<1>)
+                     : vec == 2 ? reinterpret_cast<const void *>(&adj_map_kernel<2>)
+                     : vec == 4 ? reinterpret_cast<const void *>(&adj_map_kernel<4>)
+                                : nullptr;
+    int n = 0;
+    if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 256, 0) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_adj_maps(const AdjParams &p, int vec, int blocks, cudaStream_t st)
+{
+    if (blocks < 1) return cudaErrorInvalidValue;
+    if (vec == 1) adj_map_kernel<1><<<blocks, 256, 0, st>>>(p);
+    else if (vec == 2) adj_map_kernel<2><<<blocks, 256, 0, st>>>(p);
+    else if (vec == 4) adj_map_kernel<4><<<blocks, 256, 0, st>>>(p);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_starts(const AdjParams &p, cudaStream_t st)
+{
+    int64_t blocks = ((int64_t)p.fw.T * 32 + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    adj_start_kernel<<<(int)blocks, 256, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,

@@ -34,6 +34,8 @@ struct moc_handle_s {
     size_t smlist_cap = 0;
     float *sstart = nullptr, *smap = nullptr;
     size_t sstart_cap = 0, smap_cap = 0;
+    float *sadj = nullptr;       // adjoint: lambda maps and lambda leaving each chunk
+    size_t sadj_cap = 0;
     // batching form
     float4 *bblk = nullptr;    // cell blocks of all problems of a batch
     size_t bblk_cap = 0;
@@ -183,6 +185,68 @@ moc_status_t ensure_table(moc_handle_t h, const moc_fwd_opts_t *o, cudaStream_t 
     return MOC_OK;
 }
 
+// Automatic chunk length. A lone warp takes about 260 ns per segment of its item, and the
+// whole GPU runs about 9e9 warp-segment steps per second (GB300, 32 resident warps per
+// SM): the sweep of S segments x n_gch group chunks takes S n_gch / 9e9 s. Tracks whose
+// lone time would exceed a quarter of that, L* = S n_gch / 9360 segments, are cut into
+// chunks of L* / 4 (rounded to a power of two, at least 32).
+int auto_chunk(int64_t S, int64_t n_gch)
+{
+    const double target = (double)S * (double)n_gch / 9360.0 / moc::SPLIT_MIN_FACTOR;
+    int c = 32;
+    while (c < moc::SPLIT_CHUNK_MAX && c * 1.41421356 < target) c *= 2;
+    return c;
+}
+
+// Whether long tracks are split (opts.track_chunk, and S long enough for any track to be
+// cut), and if so the split workspace, wired into *sp. Record and map counts share one
+// 64-bit scan, so both must stay below 2^31. n_gch: group chunks per track.
+moc_status_t split_setup(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
+                         int map_all, int64_t n_gch, moc::SweepParams *sp, moc::SplitWork *sw,
+                         bool *split)
+{
+    const int chunk =
+        o->track_chunk == 0 ? auto_chunk(p->n_segments, n_gch) : o->track_chunk;
+    *split = o->track_chunk != -1 && p->n_tracks > 0 &&
+             p->n_segments > (int64_t)moc::SPLIT_MIN_FACTOR * chunk &&
+             moc::split_max_records(p->n_tracks, p->n_segments, chunk) < INT32_MAX;
+    if (!*split) return MOC_OK;
+    moc_status_t s;
+    const int64_t T = p->n_tracks, Gs = p->group_stride;
+    const int64_t cap = moc::split_max_records(T, p->n_segments, chunk);
+    const int64_t nb = (T + 1023) / 1024;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->sbase), &h->sbase_cap,
+                    (size_t)(T + 1) * sizeof(int64_t))) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->sbsum), &h->sbsum_cap,
+                    (size_t)nb * sizeof(int64_t))) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->srec), &h->srec_cap,
+                    (size_t)cap * sizeof(int4))) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->smlist), &h->smlist_cap,
+                    (size_t)(cap + 1) * sizeof(int64_t))) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->sstart), &h->sstart_cap,
+                    (size_t)cap * Gs * sizeof(float))) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->smap), &h->smap_cap,
+                    2 * (size_t)cap * Gs * sizeof(float))))
+        return s;
+    sw->base = h->sbase;
+    sw->bsum = h->sbsum;
+    sw->rec = h->srec;
+    sw->map_list = h->smlist;
+    sw->n_map = h->smlist + cap;
+    sw->cap = cap;
+    sw->chunk = chunk;
+    sw->map_all = map_all;
+    sp->rec = h->srec;
+    sp->n_rec = h->sbase + T;
+    sp->map_list = sw->map_list;
+    sp->n_map = sw->n_map;
+    sp->rec_cap = cap;
+    sp->start = h->sstart;
+    sp->map_a = h->smap;
+    sp->map_b = h->smap + cap * Gs;
+    return MOC_OK;
+}
+
 // Launch configuration: groups per lane from G unless given, grid filling the GPU.
 moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
                          moc::FwdConfig *c)
@@ -269,45 +333,11 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     }
 
     // Long tracks: chunk records, the maps of non-last chunks, the chunk starts.
-    const int chunk = o->track_chunk == 0 ? moc::SPLIT_CHUNK_DEFAULT : o->track_chunk;
-    // (record and map counts share one 64-bit scan: both must stay below 2^31)
-    const bool split = o->track_chunk != -1 &&
-                       p->n_segments > (int64_t)moc::SPLIT_MIN_FACTOR * chunk &&
-                       moc::split_max_records(p->n_tracks, p->n_segments, chunk) < INT32_MAX;
     moc::SplitWork sw{};
+    bool split = false;
+    if ((s = split_setup(h, p, o, 0, sp.n_chunks, &sp, &sw, &split))) return s;
     moc::FwdConfig mcfg = cfg;
     if (split) {
-        const int64_t T = p->n_tracks, Gs = p->group_stride;
-        const int64_t cap = moc::split_max_records(T, p->n_segments, chunk);
-        const int64_t nb = (T + 1023) / 1024;
-        if ((s = ensure(h, reinterpret_cast<void **>(&h->sbase), &h->sbase_cap,
-                        (size_t)(T + 1) * sizeof(int64_t))) ||
-            (s = ensure(h, reinterpret_cast<void **>(&h->sbsum), &h->sbsum_cap,
-                        (size_t)nb * sizeof(int64_t))) ||
-            (s = ensure(h, reinterpret_cast<void **>(&h->srec), &h->srec_cap,
-                        (size_t)cap * sizeof(int4))) ||
-            (s = ensure(h, reinterpret_cast<void **>(&h->smlist), &h->smlist_cap,
-                        (size_t)(cap + 1) * sizeof(int64_t))) ||
-            (s = ensure(h, reinterpret_cast<void **>(&h->sstart), &h->sstart_cap,
-                        (size_t)cap * Gs * sizeof(float))) ||
-            (s = ensure(h, reinterpret_cast<void **>(&h->smap), &h->smap_cap,
-                        2 * (size_t)cap * Gs * sizeof(float))))
-            return s;
-        sw.base = h->sbase;
-        sw.bsum = h->sbsum;
-        sw.rec = h->srec;
-        sw.map_list = h->smlist;
-        sw.n_map = h->smlist + cap;
-        sw.cap = cap;
-        sw.chunk = chunk;
-        sp.rec = h->srec;
-        sp.n_rec = h->sbase + T;
-        sp.map_list = sw.map_list;
-        sp.n_map = sw.n_map;
-        sp.rec_cap = cap;
-        sp.start = h->sstart;
-        sp.map_a = h->smap;
-        sp.map_b = h->smap + cap * Gs;
         mcfg.mode = 1;
         mcfg.prefetch = (cfg.prefetch == moc::RING_DEPTH && cfg.store == moc::STORE_F32)
                             ? moc::RING_DEPTH
@@ -578,6 +608,7 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->sbsum) cudaFree(h->sbsum);
     if (h->srec) cudaFree(h->srec);
     if (h->smlist) cudaFree(h->smlist);
+    if (h->sadj) cudaFree(h->sadj);
     if (h->sstart) cudaFree(h->sstart);
     if (h->smap) cudaFree(h->smap);
     if (h->bblk) cudaFree(h->bblk);
@@ -809,12 +840,30 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     sp.weight = o->weight;
     sp.err = h->err;
     sp.counter = h->counter;
-    // The reverse sweep carries more work per segment than the forward: with few tracks
-    // (fewer warps than about two per SM slot) split the groups finer for parallelism.
+    // Long tracks: every chunk of a split track gets its maps, then psi entering and
+    // lambda leaving it.
+    moc::SplitWork sw{};
+    bool split = false;
+    {
+        const int v0 = o->vec ? o->vec : moc::auto_vec(p->n_groups);
+        const int64_t n_gch = (p->n_groups + 32 * v0 - 1) / (32 * v0);
+        if ((s = split_setup(h, p, o, 1, n_gch, &sp, &sw, &split))) return s;
+    }
+    if (split) {
+        const size_t n = 2 * (size_t)sw.cap * p->group_stride;
+        if ((s = ensure(h, reinterpret_cast<void **>(&h->sadj), &h->sadj_cap,
+                        n * sizeof(float))))
+            return s;
+        ap.map_c = h->sadj;
+        ap.lam_end = h->sadj + (size_t)sw.cap * p->group_stride;
+        ap.base = sw.base;
+    }
+    // The reverse sweep carries more work per segment than the forward: with few work
+    // items (fewer warps than about two per SM slot) split the groups finer.
+    const int64_t units = split ? sw.cap : p->n_tracks;
     int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
     while (!o->vec && vec > 1 &&
-           (int64_t)p->n_tracks * ((p->n_groups + 32 * vec - 1) / (32 * vec)) <
-               (int64_t)h->sm_count * 64)
+           units * ((p->n_groups + 32 * vec - 1) / (32 * vec)) < (int64_t)h->sm_count * 64)
         vec /= 2;
     sp.n_chunks = (p->n_groups + 32 * vec - 1) / (32 * vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
@@ -851,6 +900,18 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     MOC_CUDA(h, cudaMemsetAsync(h->gblk, 0, nff * sizeof(float4), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     int launches = 1;
+    if (split) {
+        const int bm = moc::adj_map_blocks_per_sm(vec);
+        if (bm < 1) return MOC_ERR_UNSUPPORTED;
+        MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, 2 * sizeof(unsigned long long), st));
+        MOC_CUDA(h, moc::launch_split_records(sp, sw, st));
+        moc::AdjParams mp = ap;
+        mp.fw.counter = h->counter + 1;
+        MOC_CUDA(h, moc::launch_adj_maps(mp, vec, bm * h->sm_count, st));
+        MOC_CUDA(h, moc::launch_adj_starts(ap, st));
+        launches += 5;
+    }
+    if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[4], st));
     if (p->n_tracks > 0) {
         const int bf = moc::adj_blocks_per_sm(vec, false), br = moc::adj_blocks_per_sm(vec, true);
         if (bf < 1 || br < 1) return MOC_ERR_UNSUPPORTED;
@@ -867,7 +928,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
         MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
         h->timed_launches = launches + 1;
         h->timed_finish = true;
-        h->timed_split = false;
+        h->timed_split = split;
     }
     return MOC_OK;
 }

@@ -46,8 +46,8 @@ enum : int32_t {
     CHUNK_LEN_MASK = 0x0fffffff,
     CHUNK_SINGLE = 1 << 30,  // the whole track: psi read and written in place
     CHUNK_LAST = 1 << 29,    // a split track's last chunk: writes the track's psi
+    CHUNK_FIRST = 1 << 28,   // a split track's first chunk
 };
-constexpr int SPLIT_CHUNK_DEFAULT = 256;  // chunk length of split tracks
 constexpr int SPLIT_MIN_FACTOR = 4;       // tracks longer than 4 chunks are split
 constexpr int SPLIT_CHUNK_MAX = 1 << 24;
 
@@ -91,6 +91,8 @@ struct SplitWork {
     int64_t cap;      // split_max_records(); offsets that are not a partition of [0, S]
                       // can ask for more: those records are dropped and reported
     int32_t chunk;
+    int32_t map_all;  // 0: the map list holds the non-last chunks (forward); 1: every
+                      // chunk of a split track (adjoint)
 };
 // Upper bound on the records of a problem (tracks + S / chunk).
 int64_t split_max_records(int64_t T, int64_t S, int chunk);
@@ -194,12 +196,21 @@ struct AdjParams {
     const float *v;          // [T][Gs]   dL/dpsi_out
     float4 *gblk;            // [R*I][Gs] (dL/dsigT, dL/da0, dL/da1, dL/da2) per cell
     float *dpsi_in;          // [T][Gs]   dL/dpsi_in (out)
+    // split tracks (fw.rec != null): fw.start / fw.map_a / fw.map_b as the forward's, and
+    float *map_c;            // [records][Gs] lambda_in = a lambda_out + c of each chunk
+    float *lam_end;          // [records][Gs] lambda leaving each chunk
+    const int64_t *base;     // [T + 1] first record of each track
 };
 // Forward pass that records psi entering every segment, then the reverse sweep that
 // scatters the cell-block gradients; vec in {1, 2, 4}.
 cudaError_t launch_adj_forward(const AdjParams &p, int vec, int blocks, cudaStream_t st);
 cudaError_t launch_adj_reverse(const AdjParams &p, int vec, int blocks, cudaStream_t st);
 int adj_blocks_per_sm(int vec, bool reverse);
+// Split tracks: (a, b, c) of every chunk of a split track (the map list, fw.counter is the
+// queue head), then psi entering and lambda leaving every chunk.
+cudaError_t launch_adj_maps(const AdjParams &p, int vec, int blocks, cudaStream_t st);
+cudaError_t launch_adj_starts(const AdjParams &p, cudaStream_t st);
+int adj_map_blocks_per_sm(int vec);
 // dL/dsigT[r][g] = sum over intervals of the sigT gradients; dL/dsource through the
 // transpose of the axial fit (jac[type][k][m]: d q_k / d y_{i+m-1}, type 0 = first
 // interval, 1 = interior, 2 = last), q1 = a1 / mu and q2 = a2 / mu2.

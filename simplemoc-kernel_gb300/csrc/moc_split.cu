@@ -7,7 +7,8 @@
 // psi = 0. A track of more than SPLIT_MIN_FACTOR * C segments is cut into chunks of C
 // segments (the last one shorter):
 //   1. records: an exclusive scan of the chunk counts of the tracks, one record per chunk;
-//   2. maps: the sweep kernel in map mode composes (a, b) of every non-last chunk;
+//   2. maps: the sweep kernel in map mode composes (a, b) of every non-last chunk (the
+//      records pass lists them; for the adjoint it lists every chunk of a split track);
 //   3. starts: per track and group, psi entering each chunk, start_0 = psi_in,
 //      start_{k+1} = a_k start_k + b_k;
 //   4. the sweep runs every chunk from its start, with tallies, all chunks at once; a
@@ -42,11 +43,18 @@ __device__ __forceinline__ int64_t count_of(const SweepParams &P, const SplitWor
     return n < W.cap ? n : W.cap;
 }
 
-// Records and map items (non-last chunks) of a track, packed for one scan: maps in the
-// high 32 bits, records in the low 32 (both totals stay below 2^32: the host caps them).
-__device__ __forceinline__ int64_t packed_count(int64_t n)
+// Map items of a track with n records: its non-last chunks (forward) or all its chunks
+// (adjoint); none for a whole track.
+__device__ __forceinline__ int64_t maps_of(int64_t n, int map_all)
 {
-    return ((n > 1 ? n - 1 : 0) << 32) | n;
+    return n > 1 ? (map_all ? n : n - 1) : 0;
+}
+
+// Records and map items of a track, packed for one scan: maps in the high 32 bits,
+// records in the low 32 (both totals stay below 2^31: the host caps them).
+__device__ __forceinline__ int64_t packed_count(int64_t n, int map_all)
+{
+    return (maps_of(n, map_all) << 32) | n;
 }
 
 // Inclusive scan of v over the block; *total = the block's sum. Called by every thread.
@@ -80,7 +88,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) scan_sums_kernel(const SweepParams
 {
     const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
     int64_t total;
-    block_incl_scan(t < P.T ? packed_count(count_of(P, W, t)) : 0, &total);
+    block_incl_scan(t < P.T ? packed_count(count_of(P, W, t), W.map_all) : 0, &total);
     if (threadIdx.x == 0) W.bsum[blockIdx.x] = total;
 }
 
@@ -105,7 +113,8 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
 {
     const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
     const int64_t n = t < P.T ? count_of(P, W, t) : 0;
-    const int64_t pk = packed_count(n);
+    const int64_t pk = packed_count(n, W.map_all);
+    const int64_t nm = maps_of(n, W.map_all);
     int64_t total;
     const int64_t incl = block_incl_scan(pk, &total);
     if (t >= P.T) return;
@@ -114,9 +123,9 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
     W.base[t] = b;
     if (t == P.T - 1) {
         W.base[P.T] = b + n;
-        *W.n_map = mb + (n > 1 ? n - 1 : 0);
+        *W.n_map = mb + nm;
     }
-    for (int64_t k = 0; k + 1 < n; k++)
+    for (int64_t k = 0; k < nm; k++)
         if (b + k < W.cap && mb + k < W.cap) W.map_list[mb + k] = b + k;
     const int64_t a = P.off[t], e = P.off[t + 1];
     bool dropped = false;
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
         for (int64_t k = 0; k < n; k++) {
             const int64_t beg = a + k * C;
             const int64_t len = k + 1 < n ? C : e - beg;
-            put(b + k, beg, len, k + 1 < n ? 0 : CHUNK_LAST);
+            put(b + k, beg, len, (k + 1 < n ? 0 : CHUNK_LAST) | (k == 0 ? CHUNK_FIRST : 0));
         }
     }
     if (dropped) atomicOr(P.err, DEVERR_OFFSETS);

@@ -23,13 +23,13 @@ def loss_weights(hp, seed=SEED):
     return w, v
 
 
-def gpu_adjoint(handle, hp, w, v):
+def gpu_adjoint(handle, hp, w, v, opts=None):
     import torch
 
     dp = mocatt.DeviceProblem(hp)
     wt = torch.from_numpy(w).cuda()
     vt = torch.from_numpy(v).cuda()
-    ds, dsrc, dpsi = handle.adj(dp, wt, vt)
+    ds, dsrc, dpsi = handle.adj(dp, wt, vt, opts)
     assert handle.synchronize() == 0
     # the incoming psi is only read
     np.testing.assert_array_equal(dp.to_host("psi"), hp.psi)
@@ -50,11 +50,20 @@ def adj_problem():
     return hp, w, v
 
 
-def test_adjoint_vs_fp64_cpu_adjoint(handle, adj_problem):
+@pytest.fixture(scope="module")
+def adj_ref(adj_problem):
+    hp, w, v = adj_problem
+    return oracle.adj_fp64(hp, w.astype(np.float64), v.astype(np.float64))
+
+
+# -1: one pass per track; 0: tracks of more than 1024 segments cut into 256-segment
+# chunks; 32: tracks of more than 128 segments cut into 32-segment chunks
+@pytest.mark.parametrize("chunk", [-1, 0, 32])
+def test_adjoint_vs_fp64_cpu_adjoint(handle, adj_problem, adj_ref, chunk):
     hp, w, v = adj_problem
     assert 1.8e6 < hp.S < 2.2e6
-    ds, dsrc, dpsi = gpu_adjoint(handle, hp, w, v)
-    ref = oracle.adj_fp64(hp, w.astype(np.float64), v.astype(np.float64))
+    ds, dsrc, dpsi = gpu_adjoint(handle, hp, w, v, mocatt.default_opts(track_chunk=chunk))
+    ref = adj_ref
     G = hp.G
     out = {k: rel(a[:, :G], ref[r][:, :G]) for k, a, r in (
         ("sigT", ds, "d_sigT"), ("source", dsrc, "d_source"), ("psi_in", dpsi, "d_psi_in"))}
@@ -62,6 +71,17 @@ def test_adjoint_vs_fp64_cpu_adjoint(handle, adj_problem):
     for k, (mx, rms) in out.items():
         assert rms <= 1e-4, (k, mx, rms)
         assert mx <= 1e-2, (k, mx, rms)
+
+
+def test_adjoint_split_keeps_whole_tracks_bitwise(handle, adj_problem):
+    """Tracks of at most 4 chunks run the one-pass arithmetic: their dL/dpsi_in equals the
+    unsplit run bit for bit."""
+    hp, w, v = adj_problem
+    _, _, d_one = gpu_adjoint(handle, hp, w, v, mocatt.default_opts(track_chunk=-1))
+    _, _, d_cut = gpu_adjoint(handle, hp, w, v, mocatt.default_opts(track_chunk=64))
+    whole = np.diff(hp.track_offsets) <= 4 * 64
+    assert whole.any() and (~whole).any()
+    assert np.array_equal(d_cut[whole], d_one[whole])
 
 
 def test_adjoint_vs_central_differences(handle, adj_problem):
@@ -140,6 +160,48 @@ def test_gradcheck_through_autograd_function(handle):
     # the kernel's FP32 atomic accumulation order varies between runs: nondet_tol
     assert torch.autograd.gradcheck(SweepLoss.apply, (sig, src, psi), eps=1e-6, atol=1e-5,
                                     rtol=1e-3, nondet_tol=1e-3)
+
+
+def test_gradcheck_split_tracks(handle):
+    """gradcheck as above on three tracks of 150-400 segments cut into 32-segment chunks:
+    the chunk maps, the psi / lambda scans over chunks and the chunked passes."""
+    import torch
+
+    hp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"].with_(
+        regions=3, groups=4, tracks=3, lognormal=(250.0, 0.4, 150, 400)))
+    assert hp.S > 4 * 32 and np.diff(hp.track_offsets).min() > 4 * 32
+    w, v = loss_weights(hp, seed=11)
+    w64, v64 = w.astype(np.float64), v.astype(np.float64)
+    opts = mocatt.default_opts(track_chunk=32)
+
+    class SweepLoss(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, sig, src, psi_in):
+            ctx.save_for_backward(sig, src, psi_in)
+            L = oracle.loss_fp64(hp, sig.detach().cpu().numpy(), src.detach().cpu().numpy(),
+                                 psi_in.detach().cpu().numpy(), w64, v64)
+            return torch.tensor(L, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gL):
+            sig, src, psi_in = ctx.saved_tensors
+            q = hp.copy()
+            q.sigT = sig.detach().cpu().numpy().astype(np.float32)
+            q.source = src.detach().cpu().numpy().astype(np.float32)
+            q.psi = psi_in.detach().cpu().numpy().astype(np.float32)
+            ds, dsrc, dpsi = gpu_adjoint(handle, q, w, v, opts)
+            g = float(gL)
+            return (torch.from_numpy(ds).double() * g, torch.from_numpy(dsrc).double() * g,
+                    torch.from_numpy(dpsi).double() * g)
+
+    sig = torch.from_numpy(hp.sigT.astype(np.float64)).requires_grad_()
+    src = torch.from_numpy(hp.source.astype(np.float64)).requires_grad_()
+    psi = torch.from_numpy(hp.psi.astype(np.float64)).requires_grad_()
+    # repeated backward calls differ by the FP32 atomic order of the gradient sums: a few
+    # hundred terms per entry, so 1e-5 of the largest gradient
+    scale = max(float(np.abs(g).max()) for g in gpu_adjoint(handle, hp, w, v, opts))
+    assert torch.autograd.gradcheck(SweepLoss.apply, (sig, src, psi), eps=1e-6, atol=1e-5,
+                                    rtol=1e-3, nondet_tol=max(1e-3, 1e-5 * scale))
 
 
 def test_adjoint_rejects_table_mode(handle):

@@ -44,8 +44,10 @@ def test_batch_matches_oracle_and_single_calls(handle):
     for hp, dp in zip(hps, dps):
         psi, ff = dp.to_host("psi"), dp.to_host("fine_flux")
         parity.check_plain(psi, ff, oracle.fwd_fp64(hp), hp.G)
+        # the batched sweep runs every track in one pass: compare with single calls that
+        # do the same
         single = mocatt.DeviceProblem(hp)
-        handle.fwd(single)
+        handle.fwd(single, mocatt.default_opts(track_chunk=-1))
         assert handle.synchronize() == 0
         d = np.abs(psi[:, :hp.G].astype(np.float64) - single.to_host("psi")[:, :hp.G])
         assert np.all(d <= 1e-6 * np.abs(psi[:, :hp.G]) + 1e-30)

@@ -37,7 +37,7 @@ def lognormal(**kw):
 def long_tracks():
     hp = lognormal()
     lens = np.diff(hp.track_offsets)
-    assert lens.max() > 4 * 256  # the default chunking cuts some tracks
+    assert lens.max() > 4 * 256  # C = 256 cuts some tracks
     return hp, oracle.fwd_fp64(hp)
 
 
@@ -50,7 +50,7 @@ def test_split_matches_fp64(handle, long_tracks, chunk):
 
 def test_short_tracks_bitwise_equal_to_unsplit(handle, long_tracks):
     hp, ref = long_tracks
-    p_split, f_split = run(handle, hp, mocatt.default_opts())
+    p_split, f_split = run(handle, hp, mocatt.default_opts(track_chunk=256))
     p_one, f_one = run(handle, hp, mocatt.default_opts(track_chunk=NO_SPLIT))
     parity.check_plain(p_one, f_one, ref, hp.G)
     lens = np.diff(hp.track_offsets)
@@ -63,17 +63,29 @@ def test_short_tracks_bitwise_equal_to_unsplit(handle, long_tracks):
 
 
 def test_split_psi_depends_only_on_the_track(handle, long_tracks):
-    """Where a track is cut depends on its length alone: a sample of tracks run as their
-    own problem reproduces the full run's psi bit for bit."""
+    """With a given chunk length, where a track is cut depends on its length alone: a
+    sample of tracks run as their own problem reproduces the full run's psi bit for bit."""
     hp, _ = long_tracks
-    psi, _ = run(handle, hp, mocatt.default_opts())
+    opts = mocatt.default_opts(track_chunk=256)
+    psi, _ = run(handle, hp, opts)
     lens = np.diff(hp.track_offsets)
     order = np.argsort(-lens)
     sample = np.sort(np.concatenate([order[:12], order[-12:],
                                      np.random.default_rng(3).choice(hp.T, 24, replace=False)]))
     sample = np.unique(sample)
-    p_sub, _ = run(handle, hp.subset_tracks(sample), mocatt.default_opts())
+    p_sub, _ = run(handle, hp.subset_tracks(sample), opts)
     assert np.array_equal(p_sub, psi[sample])
+
+
+def test_auto_chunk_cuts_long_tracks_of_small_problems(handle, long_tracks):
+    """The automatic chunk length follows the problem's size: about 600,000 segments x one
+    group chunk gives C = 32 (tracks of more than 128 segments are cut) - the same psi as
+    an explicit C = 32, bit for bit."""
+    hp, ref = long_tracks
+    p_auto, f_auto = run(handle, hp, mocatt.default_opts())
+    p_32, _ = run(handle, hp, mocatt.default_opts(track_chunk=32))
+    assert np.array_equal(p_auto, p_32)
+    parity.check_plain(p_auto, f_auto, ref, hp.G)
 
 
 def test_split_deterministic(handle, long_tracks):

@@ -40,7 +40,11 @@ def test_noalloc_matches_handle_entry_point_twice(cuda, mode):
                                    table_max=10.0)
     h = mocatt.Handle(0)
     ref_dp = mocatt.DeviceProblem(hp)
-    h.fwd(ref_dp, opts)
+    # the no-allocation entry point sweeps every track in one pass: compare with the
+    # handle entry point run the same way
+    ref_opts = mocatt.MocFwdOpts.from_buffer_copy(opts)
+    ref_opts.track_chunk = -1
+    h.fwd(ref_dp, ref_opts)
     assert h.synchronize() == 0
     psi_ref, ff_ref = ref_dp.to_host("psi"), ref_dp.to_host("fine_flux")
     h.close()
