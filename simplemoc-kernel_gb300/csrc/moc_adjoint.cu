@@ -135,11 +135,13 @@ struct AdjItem {
     int t, g0, flags;
 };
 
-__device__ __forceinline__ bool adj_item(const SweepParams &P, int64_t item, int lane, int vec,
-                                         AdjItem &it)
+// Items are numbered group chunk by group chunk (see the forward sweep): item =
+// chunk * n_units + unit, n_units the tracks or records.
+__device__ __forceinline__ bool adj_item(const SweepParams &P, int64_t item, int64_t n_units,
+                                         int lane, int vec, AdjItem &it)
 {
-    const int64_t u = item / P.n_chunks;
-    const int ch = (int)(item - u * P.n_chunks);
+    const int ch = (int)(item / n_units);
+    const int64_t u = item - (int64_t)ch * n_units;
     it.g0 = (ch * 32 + lane) * vec;
     if (P.rec) {
         const int4 r = __ldg(P.rec + u);
@@ -166,12 +168,12 @@ __device__ __forceinline__ bool adj_item(const SweepParams &P, int64_t item, int
     return true;
 }
 
-// Items of a pass: tracks (or records) times group chunks.
-__device__ __forceinline__ int64_t adj_items(const SweepParams &P)
+// Units of a pass: tracks, or records of split tracks.
+__device__ __forceinline__ int64_t adj_units(const SweepParams &P)
 {
-    if (!P.rec) return P.n_items;
+    if (!P.rec) return P.T;
     const int64_t n = *P.n_rec;
-    return (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
+    return n < P.rec_cap ? n : P.rec_cap;
 }
 
 // One segment's inputs for the reverse sweep, fetched one segment ahead.
@@ -188,14 +190,14 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
-    const int64_t n_items = adj_items(P);
+    const int64_t n_units = adj_units(P), n_items = n_units * P.n_chunks;
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)n_items) break;
         AdjItem it;
-        if (!adj_item(P, (int64_t)item, lane, VEC, it)) continue;
+        if (!adj_item(P, (int64_t)item, n_units, lane, VEC, it)) continue;
         const int g0 = it.g0;
         const int64_t beg = it.beg, end = it.end;
         const int nvalid = P.G - g0;
@@ -256,14 +258,14 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
-    const int64_t n_items = adj_items(P);
+    const int64_t n_units = adj_units(P), n_items = n_units * P.n_chunks;
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)n_items) break;
         AdjItem it;
-        if (!adj_item(P, (int64_t)item, lane, VEC, it)) continue;
+        if (!adj_item(P, (int64_t)item, n_units, lane, VEC, it)) continue;
         const int g0 = it.g0;
         const int64_t beg = it.beg, end = it.end;
         const int nvalid = P.G - g0;
@@ -352,22 +354,21 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
-    int64_t n_items = 0;
-    {
-        const int64_t n = *P.n_map;
-        n_items = (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
-    }
+    int64_t n_maps = *P.n_map;
+    n_maps = n_maps < P.rec_cap ? n_maps : P.rec_cap;
+    const int64_t n_items = n_maps * P.n_chunks;
+    const int64_t n_units = adj_units(P);
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)n_items) break;
-        const int64_t m = (int64_t)item / P.n_chunks;
-        const int ch = (int)((int64_t)item - m * P.n_chunks);
+        const int ch = (int)((int64_t)item / n_maps);
+        const int64_t m = (int64_t)item - (int64_t)ch * n_maps;
         const int64_t q = P.map_list[m];
-        if ((uint64_t)q >= (uint64_t)P.rec_cap) continue;
+        if ((uint64_t)q >= (uint64_t)n_units) continue;
         AdjItem it;
-        if (!adj_item(P, q * P.n_chunks + ch, lane, VEC, it)) continue;
+        if (!adj_item(P, (int64_t)ch * n_units + q, n_units, lane, VEC, it)) continue;
         const int g0 = it.g0;
         const int64_t beg = it.beg, end = it.end;
         const int nvalid = P.G - g0;

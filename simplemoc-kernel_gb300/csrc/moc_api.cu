@@ -318,6 +318,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     moc::FwdConfig cfg;
     if ((s = pick_config(h, p, o, &cfg))) return s;
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
+    sp.group_major = 1;
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
 
     const size_t nff = (size_t)ncell * p->group_stride;

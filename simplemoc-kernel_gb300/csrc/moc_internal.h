@@ -54,6 +54,7 @@ constexpr int SPLIT_CHUNK_MAX = 1 << 24;
 // Everything a sweep launch reads. Device pointers.
 struct SweepParams {
     int32_t R, I, G, Gs, T, n_chunks;
+    int32_t group_major;          // item order: 1 group chunk by group chunk, 0 track by track
     int64_t S, n_items;
     const int64_t *off;
     const int32_t *reg;

@@ -225,18 +225,28 @@ enum : int { MODE_SWEEP = 0, MODE_MAP = 1 };
 // a split track, which starts from its precomputed psi and, if it is the track's last,
 // writes the track's psi. MODE_MAP runs the non-last chunks of split tracks from psi = 0
 // without tallies and writes (a, b) = (product of p, outgoing psi) per group.
+// Items are numbered group chunk by group chunk (all tracks or records of groups
+// [0, 32 VEC) first, ...) when P.group_major is set, so the warps in flight read one
+// group chunk's slice of every cell block and tally row, a smaller working set in L2;
+// else track by track. n_units: tracks, records or map items.
 template <int VEC, int EK, int ST, int TL, int RD, int MODE>
-__device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int lane,
-                                           const TableRef &tr, float4 *ring)
+__device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int64_t n_units,
+                                           int lane, const TableRef &tr, float4 *ring)
 {
     const int Gs = P.Gs;
-    int64_t beg, end, row_q = 0;
+    int64_t beg, end, row_q = 0, unit;
     int ch;
+    if (P.group_major) {
+        ch = (int)(item / n_units);
+        unit = item - (int64_t)ch * n_units;
+    } else {
+        unit = item / P.n_chunks;
+        ch = (int)(item - unit * P.n_chunks);
+    }
     const float *psi_in;
     float *psi_out;  // null: the chunk's outgoing psi is not kept
     if (P.rec) {
-        int64_t q = item / P.n_chunks;
-        ch = (int)(item - q * P.n_chunks);
+        int64_t q = unit;
         if constexpr (MODE == MODE_MAP) {
             q = P.map_list[q];
             if ((uint64_t)q >= (uint64_t)P.rec_cap) return;
@@ -261,8 +271,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         }
         row_q = q * Gs;
     } else {
-        const int t = (int)(item / P.n_chunks);
-        ch = (int)(item - (int64_t)t * P.n_chunks);
+        const int t = (int)unit;
         beg = P.off[t];
         end = P.off[t + 1];
         if (!(beg >= 0 && beg <= end && end <= P.S)) {
@@ -433,10 +442,11 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD * VEC * 32);
     }
     const int lane = threadIdx.x & 31;
-    int64_t n_items = P.n_items;
+    int64_t n_items = P.n_items, n_units = P.T;
     if (P.rec) {
         const int64_t n = MODE == MODE_MAP ? *P.n_map : *P.n_rec;
-        n_items = (n < P.rec_cap ? n : P.rec_cap) * P.n_chunks;
+        n_units = n < P.rec_cap ? n : P.rec_cap;
+        n_items = n_units * P.n_chunks;
     }
     if constexpr (MODE == MODE_MAP) {
         // Map items (the non-last chunks, listed by the record pass) are full chunks of
@@ -444,7 +454,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
         for (int64_t item = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
              item < n_items; item += nw)
-            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, lane, tr, ring);
+            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, n_units, lane, tr, ring);
         return;
     }
     for (;;) {
@@ -452,7 +462,7 @@ __global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
         item = __shfl_sync(FULL, item, 0);
         if (item >= (unsigned long long)n_items) break;
-        sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, lane, tr, ring);
+        sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, n_units, lane, tr, ring);
     }
 }
 
