@@ -1,11 +1,14 @@
 // moc_sweep.cu — forward segment-attenuation sweep kernels for sm_103a.
 //
-// Work decomposition: a work item is (track, chunk of 32*VEC groups). One warp owns an
+// Work decomposition: a work item is (track, chunk of 32*VEC groups), or (chunk of a
+// long track, group chunk) when long tracks are split (moc_split.cu). One warp owns an
 // item from start to end: lanes hold VEC consecutive groups each, psi stays in registers
-// for the whole track, and the warp walks the track's segments in CSR order (psi is
-// carried from one segment to the next, src/cpu/kernel.c:53). Energy groups are
-// independent, so a track's chunks are independent items. Warps take items from a
-// global queue head (one atomicAdd per item), so tracks of uneven length balance.
+// for the whole item, and the warp walks its segments in CSR order (psi is carried from
+// one segment to the next, src/cpu/kernel.c:53). Energy groups are independent, so a
+// track's group chunks are independent items. Items are numbered group chunk by group
+// chunk, so the warps in flight share one slice of the cell blocks and tally rows in L2.
+// Warps take items from a global queue head (one atomicAdd per item), so tracks of
+// uneven length balance.
 //
 // The sweep is bound by instruction issue, so everything that is not arithmetic is cut
 // down:
@@ -17,7 +20,9 @@
 //    32-segment window and forms its cell index once; the warp then only shuffles
 //    (cell, ds) per segment; the next window is loaded 32 segments ahead;
 //  * the segment loop is unrolled by two with ping-pong registers: the block of segment
-//    j+1 is loaded before segment j is computed, without register moves.
+//    j+1 is loaded before segment j is computed, without register moves; the pairs run
+//    inside each 32-segment window with 32-bit indices (table mode keeps a loop over the
+//    whole item, measured faster there).
 // Tallies go out as red.global.add.v4.f32 (one L2 request per lane, 16 bytes).
 #include "moc_device.cuh"
 #include "moc_internal.h"
@@ -326,7 +331,35 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         }
     };
 
-    if constexpr (RD == 0) {
+    if constexpr (RD < 0) {
+        // One segment ahead (ping-pong registers) with 32-bit indexing inside 32-segment
+        // descriptor windows: the pair loop runs over a window's segments, shuffling
+        // lanes k and k+1 of window A; only the pair at the window's end reaches into
+        // window B. Segments past the item's end decode to cell -1 and are skipped.
+        Blk<VEC> b0, b1;
+        int c0 = __shfl_sync(FULL, cA, 0), c1;
+        float d0 = __shfl_sync(FULL, dA, 0), d1;
+        if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+        for (; wb < end; wb += 32) {
+            const int nk = end - wb < 32 ? (int)(end - wb) : 32;
+            for (int k = 0; k < nk; k += 2) {
+                c1 = __shfl_sync(FULL, cA, k + 1);
+                d1 = __shfl_sync(FULL, dA, k + 1);
+                if (c1 >= 0 && act) load_blk<VEC, ST>(P.blk, c1 * Gs + g0, b1);
+                step(b0, c0, d0);
+                const int kn = k + 2;
+                const int cs = kn < 32 ? cA : cB;
+                const float ds_ = kn < 32 ? dA : dB;
+                c0 = __shfl_sync(FULL, cs, kn & 31);
+                d0 = __shfl_sync(FULL, ds_, kn & 31);
+                if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+                step(b1, c1, d1);
+            }
+            cA = cB;
+            dA = dB;
+            decode(P, wb + 64 + lane, end, cB, dB);
+        }
+    } else if constexpr (RD == 0) {
         // one segment ahead, in registers (ping-pong, no moves)
         Blk<VEC> b0, b1;
         int c0 = -1, c1 = -1;
@@ -500,6 +533,15 @@ const void *fwd_fn()
     return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD, MODE>);
 }
 
+// The register-prefetch loop of each exp mode, as measured fastest on GB300 (50M x 128):
+// the windowed pair loop (RD = -1) for the plain and stable math, the ping-pong loop
+// (RD = 0) for table mode.
+template <int VEC, int EK, int ST, int TL, int MODE = MODE_SWEEP>
+const void *reg_fn()
+{
+    return fwd_fn<VEC, EK, ST, TL, EK == EXPK_TABLE ? 0 : -1, MODE>();
+}
+
 // The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
 //   plain FP32 / table FP32 with FP32 atomics (the drop-in), register or ring prefetch,
 //   stable math with FP32 storage and all three tally kinds (FP32 tallies also with the
@@ -519,16 +561,16 @@ const void *pick_vec(const FwdConfig &c)
         if (c.prefetch != 1) return nullptr;
         if (c.store == STORE_F32) {
             if (c.exp_kind == EXPK_PLAIN)
-                return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, 0, MODE_MAP>();
+                return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, MODE_MAP>();
             if (c.exp_kind == EXPK_TABLE)
-                return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, 0, MODE_MAP>();
-            return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, 0, MODE_MAP>();
+                return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, MODE_MAP>();
+            return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, MODE_MAP>();
         }
         if (c.exp_kind != EXPK_STABLE) return nullptr;
         if (c.store == STORE_BF16)
-            return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, 0, MODE_MAP>();
+            return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, MODE_MAP>();
         if (c.store == STORE_F16)
-            return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32, 0, MODE_MAP>();
+            return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32, MODE_MAP>();
         return nullptr;
     }
     if (c.mode != MODE_SWEEP) return nullptr;
@@ -543,26 +585,26 @@ const void *pick_vec(const FwdConfig &c)
     }
     if (c.store == STORE_F32) {
         if (c.exp_kind == EXPK_PLAIN && c.tally == TALLY_F32)
-            return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>();
+            return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>();
         if (c.exp_kind == EXPK_TABLE && c.tally == TALLY_F32)
-            return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>();
+            return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>();
         if (c.exp_kind == EXPK_STABLE) {
-            if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>();
-            if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>();
-            if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>();
+            if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>();
+            if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>();
+            if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>();
         }
         return nullptr;
     }
     if (c.exp_kind != EXPK_STABLE) return nullptr;
     if (c.store == STORE_BF16) {
-        if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>();
-        if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>();
-        if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F64>();
+        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>();
+        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>();
+        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F64>();
     }
     if (c.store == STORE_F16) {
-        if (c.tally == TALLY_F32) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32>();
-        if (c.tally == TALLY_COMP) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_COMP>();
-        if (c.tally == TALLY_F64) return fwd_fn<V, EXPK_STABLE, STORE_F16, TALLY_F64>();
+        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32>();
+        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_COMP>();
+        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F64>();
     }
     return nullptr;
 }
@@ -623,7 +665,7 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
 size_t fwd_smem_bytes(const FwdConfig &c, int tab_n)
 {
     size_t b = c.exp_kind == EXPK_TABLE ? (size_t)(tab_n + 1) / 2 * sizeof(float4) : 0;
-    if (c.prefetch > 1)
+    if (c.prefetch == RING_DEPTH)
         b += (size_t)c.warps_per_block * c.prefetch * c.vec * 32 * sizeof(float4);
     return b;
 }
