@@ -268,6 +268,9 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
                                                      : moc::TALLY_F32;
     }
     c->prefetch = o->prefetch > 1 ? o->prefetch : 1;
+    // the branch-free segment loop needs whole rows per lane (and the null-cell row,
+    // which fwd_device writes after the cell blocks)
+    c->branch_free = p->n_groups % vec == 0;
     const int per_sm = moc::fwd_blocks_per_sm(*c, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
     c->blocks = per_sm * h->sm_count;
@@ -279,7 +282,8 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
 {
     moc_status_t s;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
-    const size_t blk_bytes = (size_t)ncell * p->group_stride * sizeof(float4);
+    // cell blocks and the null-cell row after them
+    const size_t blk_bytes = (size_t)(ncell + 1) * p->group_stride * sizeof(float4);
     if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, blk_bytes))) return s;
     if (o->exp_mode == MOC_EXP_TABLE && (s = ensure_table(h, o, st))) return s;
 
@@ -319,6 +323,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if ((s = pick_config(h, p, o, &cfg))) return s;
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
     sp.group_major = 1;
+    sp.null_cell = (int32_t)ncell;
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
 
     const size_t nff = (size_t)ncell * p->group_stride;
@@ -356,11 +361,11 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (cfg.store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
-                                           o->mu, o->mu2, st));
+                                           o->mu, o->mu2, st, true));
     else
         MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
                                              p->n_regions, p->n_intervals, p->group_stride,
-                                             o->dz, o->zin, o->mu, o->mu2, st));
+                                             o->dz, o->zin, o->mu, o->mu2, st, true));
     if (sp.lo) MOC_CUDA(h, cudaMemsetAsync(sp.lo, 0, nff * sizeof(float), st));
     if (sp.ff64) MOC_CUDA(h, cudaMemsetAsync(sp.ff64, 0, nff * sizeof(double), st));
     // counter[0]: the sweep's queue head, counter[1]: the map pass's

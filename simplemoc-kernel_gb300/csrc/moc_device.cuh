@@ -131,6 +131,31 @@ __device__ __forceinline__ void red_row(float *p, const Vec<VEC> &t, int n_valid
     }
 }
 
+// Full-row reduction sent only where (unsigned) cell < lim: lim is R*I for a lane whose
+// groups are all real and 0 for a lane past G, so the null cell (index R*I) and idle lanes
+// send nothing. One compare and one predicated reduction, no branch.
+template <int VEC>
+__device__ __forceinline__ void red_row_if(float *p, const Vec<VEC> &t, int cell, int lim)
+{
+    if constexpr (VEC == 4) {
+        asm volatile("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %5, %6;\n\t"
+                     "@q red.global.add.v4.f32 [%0], {%1, %2, %3, %4};\n\t}"
+                     ::"l"(p), "f"(t.v[0]), "f"(t.v[1]), "f"(t.v[2]), "f"(t.v[3]), "r"(cell),
+                     "r"(lim)
+                     : "memory");
+    } else if constexpr (VEC == 2) {
+        asm volatile("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %3, %4;\n\t"
+                     "@q red.global.add.v2.f32 [%0], {%1, %2};\n\t}"
+                     ::"l"(p), "f"(t.v[0]), "f"(t.v[1]), "r"(cell), "r"(lim)
+                     : "memory");
+    } else {
+        asm volatile("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %2, %3;\n\t"
+                     "@q red.global.add.f32 [%0], %1;\n\t}"
+                     ::"l"(p), "f"(t.v[0]), "r"(cell), "r"(lim)
+                     : "memory");
+    }
+}
+
 // Compensated tally: hi[g] += t with an atomic that returns the value it added to, then
 // the exact rounding error of that addition (Knuth's TwoSum on the returned value) is
 // reduced into lo[g]. Every addition into hi is an FP32 round-to-nearest addition of the

@@ -55,6 +55,7 @@ constexpr int SPLIT_CHUNK_MAX = 1 << 24;
 struct SweepParams {
     int32_t R, I, G, Gs, T, n_chunks;
     int32_t group_major;          // item order: 1 group chunk by group chunk, 0 track by track
+    int32_t null_cell;            // R*I when blk has the null-cell row after the cells, else -1
     int64_t S, n_items;
     const int64_t *off;
     const int32_t *reg;
@@ -106,13 +107,15 @@ cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStr
 // Cell blocks of every (region, interval) and group: blk[c][g] = (sigT of the region,
 // q0, q1*mu, q2*mu2), the coefficients rounded exactly as src/cpu/kernel.c:111-191 and
 // the first product of kernel.c:250-251 / 311-322 round them.
+// null_row: also write the null cell (1, 0, 0, 0) per group after the last cell (blk
+// then holds R*I + 1 rows).
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st);
+                              cudaStream_t st, bool null_row = false);
 // The same blocks rounded to bf16 (store = STORE_BF16) or fp16 (STORE_F16), to nearest.
 cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
                                 int R, int I, int Gs, float dz, float zin, float mu,
-                                float mu2, cudaStream_t st);
+                                float mu2, cudaStream_t st, bool null_row = false);
 // fine_flux[k] = (float)((double)fine_flux[k] + lo[k]) (or + ff64[k]) over n entries.
 cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_t n,
                           cudaStream_t st);
@@ -128,6 +131,7 @@ struct FwdConfig {
     int tally = TALLY_F32;
     int prefetch = 1;     // 1: registers, one segment ahead; RING_DEPTH: cp.async ring
     int mode = 0;         // 0: the sweep; 1: affine maps of split chunks (split mode)
+    bool branch_free = false;  // the null-cell row exists and G is a multiple of vec
 };
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &cfg, cudaStream_t st);
 // Dynamic shared memory of a configuration (table of tab_n pairs in table mode + rings).

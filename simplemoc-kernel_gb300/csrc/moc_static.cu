@@ -154,6 +154,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     sp.n_chunks = (p->n_groups + 32 * cfg.vec - 1) / (32 * cfg.vec);
     sp.n_items = (int64_t)p->n_tracks * sp.n_chunks;
     sp.group_major = 1;
+    sp.null_cell = -1;  // no null-cell row in the fixed scratch: the checked segment loop
 
     NA_CUDA(moc::launch_prep_block(p->sigT, p->source, blk, p->n_regions, p->n_intervals,
                                    p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));

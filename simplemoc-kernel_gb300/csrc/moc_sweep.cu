@@ -74,15 +74,19 @@ __device__ __forceinline__ float4 cell_block(const float *__restrict__ sigT,
 
 // ST = STORE_F32 writes float4 blocks; STORE_BF16 / STORE_F16 round them to 16 bits (to
 // nearest even) and write four 16-bit values per (cell, group).
+// With null_row, the row after the last cell is the null cell: (1, 0, 0, 0) per group.
 template <int ST>
 __global__ void prep_block_kernel(const float *__restrict__ sigT,
                                   const float *__restrict__ source, void *__restrict__ blk,
-                                  int R, int I, int Gs, float dz, float zin, float mu, float mu2)
+                                  int R, int I, int Gs, float dz, float zin, float mu, float mu2,
+                                  int null_row)
 {
     const int64_t n = (int64_t)R * I * Gs;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+    const int64_t n_all = n + (null_row ? Gs : 0);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_all;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const float4 v = cell_block(sigT, source, k, I, Gs, dz, zin, mu, mu2);
+        const float4 v = k < n ? cell_block(sigT, source, k, I, Gs, dz, zin, mu, mu2)
+                               : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         if constexpr (ST == STORE_F32) {
             static_cast<float4 *>(blk)[k] = v;
         } else {
@@ -207,19 +211,24 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
 
 // Lane-parallel descriptor decode of segment j: its cell index (or -1 if the region or
 // interval is out of range, reported once through the error word) and its ds.
-__device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t end, int &cell,
-                                       float &ds)
+// A segment past the item's end or with an out-of-range index decodes to cell `none`
+// with ds = 0: -1 (skipped by the loops that test it), or the null cell R*I, whose block
+// (sigT 1, coefficients 0) makes the segment an exact no-op (p = 1, every term 0).
+__device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t end, int none,
+                                       int &cell, float &ds)
 {
-    cell = -1;
+    cell = none;
     ds = 0.0f;
     if (j < end) {
         const int r = ld_stream(P.reg + j);
         const int iv = ld_stream(P.itv + j);
-        ds = ld_stream(P.ds + j);
-        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I)
+        const float d = ld_stream(P.ds + j);
+        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I) {
             cell = r * P.I + iv;
-        else
+            ds = d;
+        } else {
             atomicOr(P.err, DEVERR_INDEX);
+        }
     }
 }
 
@@ -297,11 +306,12 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
     if (MODE == MODE_SWEEP && act) psi = ld_psi<VEC>(psi_in + g0, nvalid);
 
     // Descriptor windows: A = segments [wb, wb+32), B = the next 32.
+    const int none = RD < 0 ? P.null_cell : -1;
     int64_t wb = beg;
     int cA, cB;
     float dA, dB;
-    decode(P, wb + lane, end, cA, dA);
-    decode(P, wb + 32 + lane, end, cB, dB);
+    decode(P, wb + lane, end, none, cA, dA);
+    decode(P, wb + 32 + lane, end, none, cB, dB);
     auto desc = [&](int64_t j, int &c, float &d) {
         int k = (int)(j - wb);
         if (k >= 32) {
@@ -309,7 +319,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
             dA = dB;
             wb += 32;
             k -= 32;
-            decode(P, wb + 32 + lane, end, cB, dB);
+            decode(P, wb + 32 + lane, end, none, cB, dB);
         }
         c = __shfl_sync(FULL, cA, k);
         d = __shfl_sync(FULL, dA, k);
@@ -332,32 +342,55 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
     };
 
     if constexpr (RD < 0) {
-        // One segment ahead (ping-pong registers) with 32-bit indexing inside 32-segment
-        // descriptor windows: the pair loop runs over a window's segments, shuffling
-        // lanes k and k+1 of window A; only the pair at the window's end reaches into
-        // window B. Segments past the item's end decode to cell -1 and are skipped.
+        // Branch-free segments, one ahead (ping-pong registers), 32-bit indexing inside
+        // 32-segment descriptor windows: the pair loop shuffles lanes k and k+1 of window
+        // A; only the pair at a full window's end reaches into window B. Segments past the
+        // end or with bad indices are null-cell no-ops (decode), lanes past G read group
+        // 0's block, and the tally is one predicated reduction (red_row_if) sent only for
+        // real cells on lanes whose groups are all real (G is a multiple of VEC here).
+        const int gl = act ? g0 : 0;
+        const int lim = act ? P.null_cell : 0;
+        auto load = [&](int c, Blk<VEC> &b) { load_blk<VEC, ST>(P.blk, c * Gs + gl, b); };
+        auto step_nb = [&](const Blk<VEC> &b, int c, float d) {
+            Vec<VEC> tally, p;
+            attenuate<VEC, EK>(b, d, P.weight, tr, psi, tally, p);
+            if constexpr (MODE == MODE_MAP) {
+#pragma unroll
+                for (int k = 0; k < VEC; k++) amul.v[k] *= p.v[k];
+            } else {
+                const int idx = c * Gs + g0;
+                if constexpr (TL == TALLY_F32) {
+                    red_row_if<VEC>(P.ff + idx, tally, c, lim);
+                } else if ((unsigned)c < (unsigned)lim) {
+                    if constexpr (TL == TALLY_COMP)
+                        comp_row<VEC>(P.ff + idx, P.lo + idx, tally, VEC);
+                    else
+                        red_row_f64<VEC>(P.ff64 + idx, tally, VEC);
+                }
+            }
+        };
         Blk<VEC> b0, b1;
         int c0 = __shfl_sync(FULL, cA, 0), c1;
         float d0 = __shfl_sync(FULL, dA, 0), d1;
-        if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
+        load(c0, b0);
         for (; wb < end; wb += 32) {
             const int nk = end - wb < 32 ? (int)(end - wb) : 32;
             for (int k = 0; k < nk; k += 2) {
                 c1 = __shfl_sync(FULL, cA, k + 1);
                 d1 = __shfl_sync(FULL, dA, k + 1);
-                if (c1 >= 0 && act) load_blk<VEC, ST>(P.blk, c1 * Gs + g0, b1);
-                step(b0, c0, d0);
+                load(c1, b1);
+                step_nb(b0, c0, d0);
                 const int kn = k + 2;
                 const int cs = kn < 32 ? cA : cB;
                 const float ds_ = kn < 32 ? dA : dB;
                 c0 = __shfl_sync(FULL, cs, kn & 31);
                 d0 = __shfl_sync(FULL, ds_, kn & 31);
-                if (c0 >= 0 && act) load_blk<VEC, ST>(P.blk, c0 * Gs + g0, b0);
-                step(b1, c1, d1);
+                load(c0, b0);
+                step_nb(b1, c1, d1);
             }
             cA = cB;
             dA = dB;
-            decode(P, wb + 64 + lane, end, cB, dB);
+            decode(P, wb + 64 + lane, end, none, cB, dB);
         }
     } else if constexpr (RD == 0) {
         // one segment ahead, in registers (ping-pong, no moves)
@@ -426,7 +459,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
                 cA = cB;
                 dA = dB;
                 wb += 32;
-                decode(P, wb + 32 + lane, end, cB, dB);
+                decode(P, wb + 32 + lane, end, none, cB, dB);
             }
             const int slot = (int)((j - beg) & (RD - 1));
             issue(j + RD - 1, (slot + RD - 1) & (RD - 1));
@@ -533,13 +566,19 @@ const void *fwd_fn()
     return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD, MODE>);
 }
 
-// The register-prefetch loop of each exp mode, as measured fastest on GB300 (50M x 128):
-// the windowed pair loop (RD = -1) for the plain and stable math, the ping-pong loop
-// (RD = 0) for table mode.
+// The register-prefetch loop: the branch-free windowed pair loop (RD = -1) for the plain
+// and stable math where the configuration allows it (a null-cell row, G a multiple of
+// VEC), else the ping-pong loop with per-segment checks (RD = 0); table mode always takes
+// the ping-pong loop (measured faster there on GB300).
 template <int VEC, int EK, int ST, int TL, int MODE = MODE_SWEEP>
-const void *reg_fn()
+const void *reg_fn(bool branch_free)
 {
-    return fwd_fn<VEC, EK, ST, TL, EK == EXPK_TABLE ? 0 : -1, MODE>();
+    if constexpr (EK == EXPK_TABLE) {
+        return fwd_fn<VEC, EK, ST, TL, 0, MODE>();
+    } else {
+        return branch_free ? fwd_fn<VEC, EK, ST, TL, -1, MODE>()
+                           : fwd_fn<VEC, EK, ST, TL, 0, MODE>();
+    }
 }
 
 // The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
@@ -561,16 +600,16 @@ const void *pick_vec(const FwdConfig &c)
         if (c.prefetch != 1) return nullptr;
         if (c.store == STORE_F32) {
             if (c.exp_kind == EXPK_PLAIN)
-                return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, MODE_MAP>();
+                return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
             if (c.exp_kind == EXPK_TABLE)
-                return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, MODE_MAP>();
-            return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, MODE_MAP>();
+                return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
+            return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
         }
         if (c.exp_kind != EXPK_STABLE) return nullptr;
         if (c.store == STORE_BF16)
-            return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, MODE_MAP>();
+            return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, MODE_MAP>(c.branch_free);
         if (c.store == STORE_F16)
-            return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32, MODE_MAP>();
+            return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32, MODE_MAP>(c.branch_free);
         return nullptr;
     }
     if (c.mode != MODE_SWEEP) return nullptr;
@@ -585,26 +624,26 @@ const void *pick_vec(const FwdConfig &c)
     }
     if (c.store == STORE_F32) {
         if (c.exp_kind == EXPK_PLAIN && c.tally == TALLY_F32)
-            return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>();
+            return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>(c.branch_free);
         if (c.exp_kind == EXPK_TABLE && c.tally == TALLY_F32)
-            return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>();
+            return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>(c.branch_free);
         if (c.exp_kind == EXPK_STABLE) {
-            if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>();
-            if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>();
-            if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>();
+            if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>(c.branch_free);
+            if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>(c.branch_free);
+            if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>(c.branch_free);
         }
         return nullptr;
     }
     if (c.exp_kind != EXPK_STABLE) return nullptr;
     if (c.store == STORE_BF16) {
-        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>();
-        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>();
-        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F64>();
+        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>(c.branch_free);
+        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>(c.branch_free);
+        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F64>(c.branch_free);
     }
     if (c.store == STORE_F16) {
-        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32>();
-        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_COMP>();
-        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F64>();
+        if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F32>(c.branch_free);
+        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_COMP>(c.branch_free);
+        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F16, TALLY_F64>(c.branch_free);
     }
     return nullptr;
 }
@@ -628,27 +667,27 @@ static int grid_for(int64_t n)
 
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st)
+                              cudaStream_t st, bool null_row)
 {
-    const int64_t n = (int64_t)R * I * Gs;
+    const int64_t n = (int64_t)R * I * Gs + (null_row ? Gs : 0);
     if (n == 0) return cudaSuccess;
     prep_block_kernel<STORE_F32><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs, dz,
-                                                               zin, mu, mu2);
+                                                               zin, mu, mu2, null_row);
     return cudaGetLastError();
 }
 
 cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
                                 int R, int I, int Gs, float dz, float zin, float mu,
-                                float mu2, cudaStream_t st)
+                                float mu2, cudaStream_t st, bool null_row)
 {
-    const int64_t n = (int64_t)R * I * Gs;
+    const int64_t n = (int64_t)R * I * Gs + (null_row ? Gs : 0);
     if (n == 0) return cudaSuccess;
     if (store == STORE_BF16)
         prep_block_kernel<STORE_BF16><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
-                                                                    dz, zin, mu, mu2);
+                                                                    dz, zin, mu, mu2, null_row);
     else if (store == STORE_F16)
         prep_block_kernel<STORE_F16><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
-                                                                   dz, zin, mu, mu2);
+                                                                   dz, zin, mu, mu2, null_row);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();

@@ -35,7 +35,7 @@ def test_plain_sweep_1M_g64_full_size(handle):
     print(res, parity.rel_err(psi[:, :hp.G], p32[:, :hp.G]))
 
 
-@pytest.mark.parametrize("G", [1, 3, 16, 32, 64, 70, 128, 130, 256])
+@pytest.mark.parametrize("G", [1, 3, 16, 32, 33, 64, 65, 70, 128, 129, 130, 256])
 def test_plain_group_counts(handle, G):
     hp = small(groups=G)
     psi, ff = run_gpu(handle, hp)
