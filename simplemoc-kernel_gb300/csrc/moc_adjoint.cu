@@ -86,21 +86,29 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
     return r;
 }
 
-// psi' of one segment (stable terms), for the recording forward pass.
+// psi' of one segment, for the recording pass and the chunk maps: the forward sweep's
+// arithmetic (one ex2.approx for p, e = 1 - p). psi only needs the forward's FP32
+// accuracy, which the plain exponential meets; the cancelling derivative terms of the
+// reverse pass come from their Taylor sums (adj_terms). Also returns p and e/s.
 template <int VEC>
-__device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VEC> &psi)
+__device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VEC> &psi,
+                                        Vec<VEC> &pv, Vec<VEC> &e1v)
 {
 #pragma unroll
     for (int k = 0; k < VEC; k++) {
         const float s = b[k].x, a0 = b[k].y, a1 = b[k].z, a2 = b[k].w;
         const float tau = s * ds;
-        const ExpTerms x = exp_terms_stable(tau);
+        const float p = ex2_approx(tau * -1.44269504088896341f);
+        const float e = 1.0f - p;
+        const float tme = tau - e;
         const float rs = rcp_approx(s), rs2 = rs * rs;
-        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * (rs * rs2));
-        float pn = a0 * x.e * rs;
-        pn = fmaf(a1 * x.tme, rs2, pn);
+        const float e1 = e * rs, t2 = tme * rs2;
+        const float reuse = fmaf(e1 + e1, rs2, tau * (tau - 2.0f));
+        float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);
-        psi.v[k] = fmaf(psi.v[k], x.p, pn);
+        psi.v[k] = fmaf(psi.v[k], p, pn);
+        pv.v[k] = p;
+        e1v.v[k] = e1;
     }
 }
 
@@ -243,7 +251,10 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
             }
             if (act) {
                 st_psi<VEC>(A.hist + j * Gs + g0, psi, nvalid);
-                if (c0 >= 0) advance<VEC>(b0, d0, psi);
+                if (c0 >= 0) {
+                    Vec<VEC> pv, e1v;
+                    advance<VEC>(b0, d0, psi, pv, e1v);
+                }
             }
             c0 = c1;
             d0 = d1;
@@ -348,7 +359,7 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
 // Maps of every chunk of a split track, per group: psi_out = a psi_in + b (forward) and
 // lambda_in = a lambda_out + c (reverse), with a the product of the chunk's p and
 // c = sum_j (product of p before segment j) W_j e_j / s_j, the chunk's lambda sources
-// carried to its start. The arithmetic of psi is the recording pass's (advance).
+// carried to its start. The arithmetic is the recording pass's (advance).
 template <int VEC>
 __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
 {
@@ -423,19 +434,14 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
                 }
             }
             if (act && c0 >= 0) {
+                // b is the map of psi from 0 (advance), c gathers W e/s carried back to the
+                // chunk's start by the product of p so far (a before this segment)
+                Vec<VEC> pv, e1v;
+                advance<VEC>(b0, d0, mb, pv, e1v);
 #pragma unroll
                 for (int k = 0; k < VEC; k++) {
-                    const float s = b0[k].x, a0 = b0[k].y, a1 = b0[k].z, a2 = b0[k].w;
-                    const float tau = s * d0;
-                    const ExpTerms x = exp_terms_stable(tau);
-                    const float rs = rcp_approx(s), rs2 = rs * rs;
-                    const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * (rs * rs2));
-                    float pn = a0 * x.e * rs;
-                    pn = fmaf(a1 * x.tme, rs2, pn);
-                    pn = fmaf(a2, reuse, pn);
-                    mc.v[k] = fmaf(ma.v[k], P.weight * w0.v[k] * x.e * rs, mc.v[k]);
-                    mb.v[k] = fmaf(mb.v[k], x.p, pn);
-                    ma.v[k] *= x.p;
+                    mc.v[k] = fmaf(ma.v[k], P.weight * w0.v[k] * e1v.v[k], mc.v[k]);
+                    ma.v[k] *= pv.v[k];
                 }
             }
             c0 = c1;
@@ -470,18 +476,39 @@ __global__ void adj_start_kernel(const AdjParams A)
         const int64_t e = A.base[t + 1] < P.rec_cap ? A.base[t + 1] : P.rec_cap;
         const int64_t nq = e - b;
         if (nq < 2) continue;
+        float *__restrict__ start = P.start;
+        float *__restrict__ lam_end = A.lam_end;
+        constexpr int NB = 8;  // maps loaded ahead of each scan's FMA chain
         for (int g = lane; g < P.G; g += 32) {
             float psi = P.psi[t * P.Gs + g];
-            for (int64_t k = 0; k < nq; k++) {
-                const int64_t row = (b + k) * P.Gs + g;
-                P.start[row] = psi;
-                psi = fmaf(ma[row], psi, mb[row]);
+            for (int64_t k0 = 0; k0 < nq; k0 += NB) {
+                float av[NB], bv[NB];
+#pragma unroll
+                for (int k = 0; k < NB; k++) {
+                    const int64_t row = (b + k0 + k) * P.Gs + g;
+                    av[k] = k0 + k < nq ? ma[row] : 0.0f;
+                    bv[k] = k0 + k < nq ? mb[row] : 0.0f;
+                }
+#pragma unroll
+                for (int k = 0; k < NB; k++) {
+                    if (k0 + k < nq) start[(b + k0 + k) * P.Gs + g] = psi;
+                    psi = fmaf(av[k], psi, bv[k]);
+                }
             }
             float lam = A.v[t * P.Gs + g];
-            for (int64_t k = nq - 1; k >= 0; k--) {
-                const int64_t row = (b + k) * P.Gs + g;
-                A.lam_end[row] = lam;
-                lam = fmaf(ma[row], lam, mc[row]);
+            for (int64_t k0 = nq - 1; k0 >= 0; k0 -= NB) {
+                float av[NB], cv[NB];
+#pragma unroll
+                for (int k = 0; k < NB; k++) {
+                    const int64_t row = (b + k0 - k) * P.Gs + g;
+                    av[k] = k0 - k >= 0 ? ma[row] : 0.0f;
+                    cv[k] = k0 - k >= 0 ? mc[row] : 0.0f;
+                }
+#pragma unroll
+                for (int k = 0; k < NB; k++) {
+                    if (k0 - k >= 0) lam_end[(b + k0 - k) * P.Gs + g] = lam;
+                    lam = fmaf(av[k], lam, cv[k]);
+                }
             }
         }
     }

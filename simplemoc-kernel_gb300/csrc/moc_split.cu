@@ -24,6 +24,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int SCAN_BLOCK = 1024;
+constexpr int SCAN_BATCH = 8;  // chunk maps loaded ahead of the start scan's FMA chain
 
 __device__ __forceinline__ bool track_ok(int64_t a, int64_t b, int64_t S)
 {
@@ -172,10 +173,21 @@ __global__ void split_start_kernel(const SweepParams P, const SplitWork W)
         float *__restrict__ start = P.start;
         for (int g = lane; g < P.G; g += 32) {
             float psi = P.psi[t * P.Gs + g];
-            for (int64_t c = 0; c < nq; c++) {
-                const int64_t row = (b + c) * P.Gs + g;
-                start[row] = psi;
-                if (c + 1 < nq) psi = fmaf(ma[row], psi, mb[row]);
+            // the maps of 8 chunks are loaded before their 8 dependent FMAs, so the chain
+            // waits for memory once per 8 chunks, not once per chunk
+            for (int64_t c0 = 0; c0 < nq; c0 += SCAN_BATCH) {
+                float av[SCAN_BATCH], bv[SCAN_BATCH];
+#pragma unroll
+                for (int k = 0; k < SCAN_BATCH; k++) {
+                    const int64_t row = (b + c0 + k) * P.Gs + g;
+                    av[k] = c0 + k + 1 < nq ? ma[row] : 0.0f;
+                    bv[k] = c0 + k + 1 < nq ? mb[row] : 0.0f;
+                }
+#pragma unroll
+                for (int k = 0; k < SCAN_BATCH; k++) {
+                    if (c0 + k < nq) start[(b + c0 + k) * P.Gs + g] = psi;
+                    psi = fmaf(av[k], psi, bv[k]);
+                }
             }
         }
     }
