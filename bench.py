@@ -367,6 +367,26 @@ def _time_fwd(h, dp, opts, reps=3):
     return statistics.median(ts)
 
 
+def _adjoint_vs_forward(h, dp, opts, fwd_ms, reps=3):
+    """Median device time of moc_attenuate_adj (every pass: cell blocks, split, recording,
+    reverse, finish) on a problem, against one forward sweep of it (fwd_ms)."""
+    import torch
+
+    w = torch.randn_like(dp.fine_flux)
+    v = torch.randn_like(dp.psi)
+    h.adj(dp, w, v, opts)
+    ts = []
+    for _ in range(reps):
+        h.adj(dp, w, v, opts)
+        t = h.timings()
+        ts.append(t.prep_ms + t.split_ms + t.sweep_ms + t.finish_ms)
+    if h.synchronize():
+        raise RuntimeError("device error in the adjoint")
+    adj = statistics.median(ts)
+    return {"segments": int(dp.S), "groups": int(dp.G), "forward_ms": fwd_ms,
+            "adjoint_ms": adj, "ratio": adj / fwd_ms}
+
+
 FORMS_ACCURACY = os.path.join(ROOT, "profiles", "forms_accuracy_gb300.json")
 
 
@@ -416,21 +436,14 @@ def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
                           "on the wide-tau inputs (tests/test_forms_gpu.py, recorded in "
                           "profiles/forms_accuracy_gb300.json)")
 
-    # adjoint: 5,000 lognormal tracks, ~2M segments, G = 64
+    # adjoint: on the bench problem (50M x 128, the size the adjoint's cost target is
+    # stated at) and on the gradient-check workload (5,000 lognormal tracks, ~2M
+    # segments, G = 64)
+    out["adjoint"] = {"sweep_50M_g128": _adjoint_vs_forward(h, dp, plain, t_plain)}
     ahp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"])
     adp = mocatt.DeviceProblem(ahp)
-    t_fwd = _time_fwd(h, adp, plain)
-    w = torch.randn_like(adp.fine_flux)
-    v = torch.randn_like(adp.psi)
-    h.adj(adp, w, v, plain)
-    ts = []
-    for _ in range(3):
-        h.adj(adp, w, v, plain)
-        t = h.timings()
-        ts.append(t.prep_ms + t.sweep_ms + t.finish_ms)
-    t_adj = statistics.median(ts)
-    out["adjoint"] = {"workload": "adjoint_2M_g64", "segments": ahp.S, "groups": ahp.G,
-                      "forward_ms": t_fwd, "adjoint_ms": t_adj, "ratio": t_adj / t_fwd}
+    out["adjoint"]["adjoint_2M_g64"] = _adjoint_vs_forward(h, adp, plain,
+                                                           _time_fwd(h, adp, plain))
     del adp
 
     # batching: three problems (G = 16, 70, 128), one graph-captured launch

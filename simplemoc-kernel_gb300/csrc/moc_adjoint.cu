@@ -43,16 +43,18 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
 {
     AdjTerms r;
     if (tau < 1.0f) {
-        // s4 = sum_{k>=4} (-1)^k tau^k / k! (through tau^12)
-        float h = 1.0f / 479001600.0f;
-        h = fmaf(h, -tau, 1.0f / 39916800.0f);
-        h = fmaf(h, -tau, 1.0f / 3628800.0f);
-        h = fmaf(h, -tau, 1.0f / 362880.0f);
-        h = fmaf(h, -tau, 1.0f / 40320.0f);
-        h = fmaf(h, -tau, 1.0f / 5040.0f);
-        h = fmaf(h, -tau, 1.0f / 720.0f);
-        h = fmaf(h, -tau, 1.0f / 120.0f);
-        h = fmaf(h, -tau, 1.0f / 24.0f);
+        // s4 = sum_{k>=4} (-1)^k tau^k / k! = tau^4 h, h = 1/24 - tau h5, with
+        // h5 = sum_{j>=0} (-tau)^j / (j+5)! (through tau^12) - the Horner chain's value one
+        // step before h
+        float h5 = 1.0f / 479001600.0f;
+        h5 = fmaf(h5, -tau, 1.0f / 39916800.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 3628800.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 362880.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 40320.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 5040.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 720.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 120.0f);
+        const float h = fmaf(h5, -tau, 1.0f / 24.0f);
         const float t2 = tau * tau, t3 = t2 * tau, t4 = t2 * t2;
         const float s4 = h * t4;
         r.cub = 6.0f * s4;
@@ -63,18 +65,13 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
         r.d1 = fmaf(-(tau + 2.0f), s4, t3 * fmaf(tau, 1.0f / 6.0f, -1.0f / 6.0f));
         // D2 = tau p - e = -tau^2/2 + tau^3/3 - tau^4/6 + (1 + tau) s4
         r.d2 = fmaf(1.0f + tau, s4, t2 * fmaf(tau, fmaf(tau, -1.0f / 6.0f, 1.0f / 3.0f), -0.5f));
-        // D3 = 6 sum_{m>=5} (-1)^m (m-4) tau^m / m! = -6 tau^5 sum_j (j+1) (-tau)^j / (j+5)!
-        float d = 8.0f / 479001600.0f;             // (7+1)/12!
-        d = fmaf(d, -tau, 7.0f / 39916800.0f);
-        d = fmaf(d, -tau, 6.0f / 3628800.0f);
-        d = fmaf(d, -tau, 5.0f / 362880.0f);
-        d = fmaf(d, -tau, 4.0f / 40320.0f);
-        d = fmaf(d, -tau, 3.0f / 5040.0f);
-        d = fmaf(d, -tau, 2.0f / 720.0f);
-        d = fmaf(d, -tau, 1.0f / 120.0f);
-        r.d3 = -6.0f * d * t4 * tau;
+        // D3 = tau dcub/dtau - 4 cub with dcub/dtau = tau^3 - 6 s4:
+        //    = tau^4 - (6 tau + 24) s4 = tau^5 ((6 tau + 24) h5 - 1/4)
+        // (-1/4 against ~1/5: the leading terms cancel by a factor of 5 only)
+        r.d3 = t4 * tau * fmaf(fmaf(6.0f, tau, 24.0f), h5, -0.25f);
     } else {
-        r.p = exp_neg_rr(tau);
+        // no cancellation above tau = 1: one ex2.approx
+        r.p = ex2_approx(tau * -1.44269504088896341f);
         r.e = 1.0f - r.p;
         r.tme = tau - r.e;
         r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
@@ -112,19 +109,23 @@ __device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VE
     }
 }
 
+// Segment j of [lo, hi): its cell and ds; outside the range or with a bad index, cell
+// `none` and ds = 0 (-1 to be skipped, or the null cell R*I: an exact no-op).
 __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t lo, int64_t hi,
-                                       int &cell, float &ds)
+                                       int none, int &cell, float &ds)
 {
-    cell = -1;
+    cell = none;
     ds = 0.0f;
     if (j >= lo && j < hi) {
         const int r = ld_stream(P.reg + j);
         const int iv = ld_stream(P.itv + j);
-        ds = ld_stream(P.ds + j);
-        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I)
+        const float d = ld_stream(P.ds + j);
+        if ((unsigned)r < (unsigned)P.R && (unsigned)iv < (unsigned)P.I) {
             cell = r * P.I + iv;
-        else
+            ds = d;
+        } else {
             atomicOr(P.err, DEVERR_INDEX);
+        }
     }
 }
 
@@ -193,6 +194,48 @@ struct RevSeg {
     Vec<VEC> psi, w;
 };
 
+// Full-row gradient reduction of one group, sent only where (unsigned) cell < lim (lim is
+// R*I on active lanes and 0 on idle ones; the null cell R*I sends nothing). Padding groups
+// of an active lane land in the workspace's padding, which the finish pass ignores.
+__device__ __forceinline__ void red4_if(float4 *p, const float4 &g, int cell, int lim)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %5, %6;\n\t"
+                 "@q red.global.add.v4.f32 [%0], {%1, %2, %3, %4};\n\t}"
+                 ::"l"(p), "f"(g.x), "f"(g.y), "f"(g.z), "f"(g.w), "r"(cell), "r"(lim)
+                 : "memory");
+}
+
+// The reverse sweep of one segment for VEC groups: gradient block scattered, lambda
+// carried back (lambda_in = p lambda_out + W e/s).
+template <int VEC>
+__device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg<VEC> &sg,
+                                                Vec<VEC> &lam, float4 *gb, int lim)
+{
+#pragma unroll
+    for (int q = 0; q < VEC; q++) {
+        const float s = sg.b[q].x, a0 = sg.b[q].y, a1 = sg.b[q].z, a2 = sg.b[q].w;
+        const float d = sg.d;
+        const float ps = sg.psi.v[q], la = lam.v[q], W = A.fw.weight * sg.w.v[q];
+        const float tau = s * d;
+        const AdjTerms x = adj_terms(tau);
+        const float rs = rcp_approx(s), rs2 = rs * rs, rs3 = rs2 * rs;
+        const float rs4 = rs2 * rs2, rs5 = rs4 * rs;
+        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * rs3);
+        const float dreuse = fmaf((2.0f * tau - 2.0f) * tau, rs,
+                                  fmaf(2.0f * tau, x.p, -6.0f * x.e) * rs4);
+        const float fi_s = a0 * x.d1 * rs3 + ps * x.d2 * rs2 + a1 * dreuse +
+                           a2 * x.d3 * rs5 * (1.0f / 3.0f);
+        const float pn_s = a0 * x.d2 * rs2 + a1 * x.d1 * rs3 + a2 * dreuse - ps * x.p * d;
+        float4 gr;
+        gr.x = fmaf(la, pn_s, W * fi_s);
+        gr.y = fmaf(la, x.e * rs, W * x.tme * rs2);
+        gr.z = fmaf(la, x.tme * rs2, W * reuse);
+        gr.w = fmaf(la, reuse, W * x.cub * rs4 * (1.0f / 3.0f));
+        lam.v[q] = fmaf(la, x.p, W * x.e * rs);
+        red4_if(gb + sg.c * A.fw.Gs + q, gr, sg.c, lim);
+    }
+}
+
 template <int VEC>
 __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
 {
@@ -220,8 +263,8 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
         int64_t wb = beg;
         int cA, cB;
         float dA, dB;
-        decode(P, wb + lane, beg, end, cA, dA);
-        decode(P, wb + 32 + lane, beg, end, cB, dB);
+        decode(P, wb + lane, beg, end, -1, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
         auto desc = [&](int64_t j, int &c, float &d) {
             int k = (int)(j - wb);
             if (k >= 32) {
@@ -229,7 +272,7 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
                 dA = dB;
                 wb += 32;
                 k -= 32;
-                decode(P, wb + 32 + lane, beg, end, cB, dB);
+                decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
             }
             c = __shfl_sync(FULL, cA, k);
             d = __shfl_sync(FULL, dA, k);
@@ -270,6 +313,7 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
     const SweepParams &P = A.fw;
     const int lane = threadIdx.x & 31;
     const int64_t n_units = adj_units(P), n_items = n_units * P.n_chunks;
+    const int nullc = P.null_cell;
     for (;;) {
         unsigned long long item = 0;
         if (lane == 0) item = atomicAdd(P.counter, 1ULL);
@@ -282,74 +326,53 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
         const int nvalid = P.G - g0;
         const bool act = nvalid > 0;
         const int Gs = P.Gs;
-        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        // idle lanes (groups past G) read group 0 and send nothing
+        const int gl = act ? g0 : 0;
+        const int lim = act ? nullc : 0;
+        const float4 *bb = static_cast<const float4 *>(P.blk) + gl;
+        float4 *gb = A.gblk + g0;
         const bool single = (it.flags & CHUNK_SINGLE) != 0;
         const float *lam_src = single ? A.v + (int64_t)it.t * Gs : A.lam_end + it.q * Gs;
         Vec<VEC> lam;
         if (act) lam = ld_psi<VEC>(lam_src + g0, nvalid);
-        // descriptor windows from the end: A = [wa, wa+32), B = the 32 before it
+        // Descriptor windows aligned to the item's end: A = [wa, wa+32), B = the 32 before
+        // it; segments below beg decode to the null cell (no-ops). The pair loop walks k =
+        // 31, 30, ... of window A with two fetch slots in turn (no copies); only the pair at
+        // a window's start reaches into window B.
         int64_t wa = end - 32;
         int cA, cB;
         float dA, dB;
-        decode(P, wa + lane, beg, end, cA, dA);
-        decode(P, wa - 32 + lane, beg, end, cB, dB);
-        auto fetch = [&](int64_t j, RevSeg<VEC> &sg) {
-            int k = (int)(j - wa);
-            if (k < 0) {
+        decode(P, wa + lane, beg, end, nullc, cA, dA);
+        decode(P, wa - 32 + lane, beg, end, nullc, cB, dB);
+        auto fetch = [&](int c, float d, int64_t j, RevSeg<VEC> &sg) {
+            sg.c = c;
+            sg.d = d;
+            const int64_t jl = j < beg ? beg : j;  // a null segment below beg reads row beg
+            const int cw = c < nullc ? c : 0;      // the null cell has no w row
+            load4<VEC>(bb + c * Gs, sg.b);
+            sg.psi = ld_psi<VEC>(A.hist + jl * Gs + gl, VEC);
+            sg.w = ld_psi<VEC>(A.w + cw * Gs + gl, VEC);
+        };
+        RevSeg<VEC> s0, s1;
+        if (end > beg) {
+            fetch(__shfl_sync(FULL, cA, 31), __shfl_sync(FULL, dA, 31), wa + 31, s0);
+            for (; wa + 31 >= beg; wa -= 32) {
+                const int klo = beg > wa ? (int)(beg - wa) : 0;
+                for (int k = 31; k >= klo; k -= 2) {
+                    fetch(__shfl_sync(FULL, cA, k - 1), __shfl_sync(FULL, dA, k - 1),
+                          wa + k - 1, s1);
+                    reverse_segment<VEC>(A, s0, lam, gb, lim);
+                    const int kn = k - 2;
+                    const int cs = kn >= 0 ? cA : cB;
+                    const float dsn = kn >= 0 ? dA : dB;
+                    fetch(__shfl_sync(FULL, cs, kn & 31), __shfl_sync(FULL, dsn, kn & 31),
+                          wa + kn, s0);
+                    reverse_segment<VEC>(A, s1, lam, gb, lim);
+                }
                 cA = cB;
                 dA = dB;
-                wa -= 32;
-                k += 32;
-                decode(P, wa - 32 + lane, beg, end, cB, dB);
+                decode(P, wa - 64 + lane, beg, end, nullc, cB, dB);
             }
-            sg.c = __shfl_sync(FULL, cA, k);
-            sg.d = __shfl_sync(FULL, dA, k);
-            if (sg.c >= 0 && act) {
-                load4<VEC>(bb + sg.c * Gs, sg.b);
-                sg.psi = ld_psi<VEC>(A.hist + j * Gs + g0, nvalid);
-                sg.w = ld_psi<VEC>(A.w + sg.c * Gs + g0, nvalid);
-            }
-        };
-        RevSeg<VEC> cur, nxt;
-        cur.c = -1;
-        if (end > beg) fetch(end - 1, cur);
-        for (int64_t j = end - 1; j >= beg; j--) {
-            nxt.c = -1;
-            if (j - 1 >= beg) fetch(j - 1, nxt);
-            const int c = cur.c;
-            if (act && c >= 0) {
-                const float d = cur.d;
-#pragma unroll
-                for (int q = 0; q < VEC; q++) {
-                    const float s = cur.b[q].x, a0 = cur.b[q].y, a1 = cur.b[q].z,
-                                a2 = cur.b[q].w;
-                    const float ps = cur.psi.v[q], la = lam.v[q], W = P.weight * cur.w.v[q];
-                    const float tau = s * d;
-                    const AdjTerms x = adj_terms(tau);
-                    const float rs = rcp_approx(s), rs2 = rs * rs, rs3 = rs2 * rs;
-                    const float rs4 = rs2 * rs2, rs5 = rs4 * rs;
-                    const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * rs3);
-                    const float dreuse = fmaf((2.0f * tau - 2.0f) * tau, rs,
-                                              fmaf(2.0f * tau, x.p, -6.0f * x.e) * rs4);
-                    const float fi_s = a0 * x.d1 * rs3 + ps * x.d2 * rs2 + a1 * dreuse +
-                                       a2 * x.d3 * rs5 * (1.0f / 3.0f);
-                    const float pn_s = a0 * x.d2 * rs2 + a1 * x.d1 * rs3 + a2 * dreuse -
-                                       ps * x.p * d;
-                    float4 gr;
-                    gr.x = fmaf(la, pn_s, W * fi_s);
-                    gr.y = fmaf(la, x.e * rs, W * x.tme * rs2);
-                    gr.z = fmaf(la, x.tme * rs2, W * reuse);
-                    gr.w = fmaf(la, reuse, W * x.cub * rs4 * (1.0f / 3.0f));
-                    lam.v[q] = fmaf(la, x.p, W * x.e * rs);
-                    if (q < nvalid) {
-                        float *g = reinterpret_cast<float *>(A.gblk + c * Gs + g0 + q);
-                        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(g),
-                                     "f"(gr.x), "f"(gr.y), "f"(gr.z), "f"(gr.w)
-                                     : "memory");
-                    }
-                }
-            }
-            cur = nxt;
         }
         if (act && (single || (it.flags & CHUNK_FIRST)))
             st_psi<VEC>(A.dpsi_in + (int64_t)it.t * Gs + g0, lam, nvalid);
@@ -396,8 +419,8 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
         int64_t wb = beg;
         int cA, cB;
         float dA, dB;
-        decode(P, wb + lane, beg, end, cA, dA);
-        decode(P, wb + 32 + lane, beg, end, cB, dB);
+        decode(P, wb + lane, beg, end, -1, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
         auto desc = [&](int64_t j, int &c, float &d) {
             int k = (int)(j - wb);
             if (k >= 32) {
@@ -405,7 +428,7 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
                 dA = dB;
                 wb += 32;
                 k -= 32;
-                decode(P, wb + 32 + lane, beg, end, cB, dB);
+                decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
             }
             c = __shfl_sync(FULL, cA, k);
             d = __shfl_sync(FULL, dA, k);
@@ -458,9 +481,11 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
     }
 }
 
-// psi entering and lambda leaving every chunk of the split tracks: one warp per track,
-// lanes over groups. psi_0 = psi_in, psi_{k+1} = a_k psi_k + b_k; lambda leaving the last
-// chunk = dL/dpsi_out, lambda leaving chunk k-1 = a_k lambda_k + c_k.
+// psi entering and lambda leaving every chunk of the split tracks. One warp per (track,
+// 32-group slice, direction), lanes over groups: psi_0 = psi_in, psi_{k+1} = a_k psi_k +
+// b_k forwards; lambda leaving the last chunk = dL/dpsi_out, lambda leaving chunk k-1 =
+// a_k lambda_k + c_k backwards. The maps of 8 chunks are loaded ahead of their 8
+// dependent FMAs.
 __global__ void adj_start_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
@@ -469,17 +494,23 @@ __global__ void adj_start_kernel(const AdjParams A)
     const float *__restrict__ ma = P.map_a;
     const float *__restrict__ mb = P.map_b;
     const float *__restrict__ mc = A.map_c;
-    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < P.T;
-         t += nwarps) {
+    float *__restrict__ start = P.start;
+    float *__restrict__ lam_end = A.lam_end;
+    constexpr int NB = 8;
+    const int nsl = (P.G + 31) / 32;
+    const int64_t units = (int64_t)P.T * nsl * 2;
+    for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units;
+         u += nwarps) {
+        const int64_t t = u / (2 * nsl);
+        const int rest = (int)(u - t * 2 * nsl);
+        const int sl = rest >> 1, dir = rest & 1;
         const int64_t b = A.base[t];
         if (b >= P.rec_cap) continue;
         const int64_t e = A.base[t + 1] < P.rec_cap ? A.base[t + 1] : P.rec_cap;
         const int64_t nq = e - b;
-        if (nq < 2) continue;
-        float *__restrict__ start = P.start;
-        float *__restrict__ lam_end = A.lam_end;
-        constexpr int NB = 8;  // maps loaded ahead of each scan's FMA chain
-        for (int g = lane; g < P.G; g += 32) {
+        const int g = sl * 32 + lane;
+        if (nq < 2 || g >= P.G) continue;
+        if (dir == 0) {
             float psi = P.psi[t * P.Gs + g];
             for (int64_t k0 = 0; k0 < nq; k0 += NB) {
                 float av[NB], bv[NB];
@@ -495,6 +526,7 @@ __global__ void adj_start_kernel(const AdjParams A)
                     psi = fmaf(av[k], psi, bv[k]);
                 }
             }
+        } else {
             float lam = A.v[t * P.Gs + g];
             for (int64_t k0 = nq - 1; k0 >= 0; k0 -= NB) {
                 float av[NB], cv[NB];
@@ -616,7 +648,8 @@ cudaError_t launch_adj_maps(const AdjParams &p, int vec, int blocks, cudaStream_
 
 cudaError_t launch_adj_starts(const AdjParams &p, cudaStream_t st)
 {
-    int64_t blocks = ((int64_t)p.fw.T * 32 + 255) / 256;
+    const int64_t warps = (int64_t)p.fw.T * ((p.fw.G + 31) / 32) * 2;
+    int64_t blocks = (warps * 32 + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
     adj_start_kernel<<<(int)blocks, 256, 0, st>>>(p);

@@ -821,7 +821,9 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
 
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
     const size_t nff = (size_t)ncell * p->group_stride;
-    if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, nff * sizeof(float4))))
+    // cell blocks and the null-cell row after them
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap,
+                    (nff + p->group_stride) * sizeof(float4))))
         return s;
     if ((s = ensure(h, reinterpret_cast<void **>(&h->gblk), &h->gblk_cap, nff * sizeof(float4))))
         return s;
@@ -842,6 +844,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     sp.itv = p->seg_interval;
     sp.ds = p->seg_ds;
     sp.blk = h->blk;
+    sp.null_cell = (int32_t)ncell;
     sp.psi = p->psi;
     sp.weight = o->weight;
     sp.err = h->err;
@@ -902,7 +905,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
     MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                        p->n_intervals, p->group_stride, o->dz, o->zin, o->mu,
-                                       o->mu2, st));
+                                       o->mu2, st, true));
     MOC_CUDA(h, cudaMemsetAsync(h->gblk, 0, nff * sizeof(float4), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     int launches = 1;
