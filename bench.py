@@ -47,9 +47,9 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 # Algorithmic L2 bytes per segment*group of the plain FP32 sweep: the cell block
 # (sigT, q0, q1*mu, q2*mu2) 16 B + the segment descriptor 9 B / G gathered, and the tally
-# 4 B reduced. FP32 instructions per segment*group of the plain arithmetic (27, counted
+# 4 B reduced. FP32 instructions per segment*group of the plain arithmetic (25, counted
 # from attenuate<> in csrc/moc_sweep.cu) and MUFU operations (ex2 + rcp).
-FP32_OPS_PER_UNIT = 27
+FP32_OPS_PER_UNIT = 25
 MUFU_OPS_PER_UNIT = 2
 
 

@@ -133,7 +133,8 @@ typedef struct {
                                      and return MOC_ERR_BAD_INDEX without touching
                                      fine_flux or psi                                     */
     int32_t vec;                  /* groups per lane: 0 = auto, else 1, 2 or 4          */
-    int32_t warps_per_block;      /* 0 = auto, else 1..8                                */
+    int32_t warps_per_block;      /* 0 = auto (8; 16 in table mode), else 1..16 (the
+                                     batching form: 1..8)                                 */
     int32_t profile;              /* 1: time each kernel of the call with CUDA events on
                                      the call's stream (read with moc_last_timings)      */
     int32_t prefetch;             /* segments whose cell blocks are in flight ahead of the

@@ -118,7 +118,7 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         (o->table_points < 2 || o->table_points > 24000 || !(o->table_max > 0.0f)))
         return MOC_ERR_INVALID_ARG;
     if (o->vec != 0 && o->vec != 1 && o->vec != 2 && o->vec != 4) return MOC_ERR_INVALID_ARG;
-    if (o->warps_per_block < 0 || o->warps_per_block > 8) return MOC_ERR_INVALID_ARG;
+    if (o->warps_per_block < 0 || o->warps_per_block > 16) return MOC_ERR_INVALID_ARG;
     if (o->prefetch != 0 && o->prefetch != 1 && o->prefetch != moc::RING_DEPTH)
         return MOC_ERR_INVALID_ARG;
     if (o->track_chunk != 0 && o->track_chunk != -1 &&
@@ -254,8 +254,9 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
     int vec = o->vec;
     if (vec == 0) vec = moc::auto_vec(p->n_groups);
     c->vec = vec;
-    c->warps_per_block = o->warps_per_block ? o->warps_per_block : 8;
     c->exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+    c->warps_per_block =
+        o->warps_per_block ? o->warps_per_block : moc::auto_warps_per_block(c->exp_kind);
     c->store = moc::STORE_F32;
     c->tally = moc::TALLY_F32;
     if (o->precision != MOC_PREC_FP32) {

@@ -128,15 +128,16 @@ __device__ __forceinline__ void attenuate_b(const float4 (&x)[VEC], float ds, fl
             e = 1.0f - p;
         }
         // same arithmetic as the single-problem sweep (attenuate<> in moc_sweep.cu)
+        const float tt = tau * tau;
         const float tme = tau - e;
-        const float cub = fmaf(tau * tau, tau - 3.0f, 6.0f * tme);
+        const float cub3 = fmaf(tt, fmaf(tau, 1.0f / 3.0f, -1.0f), tme + tme);
         const float rs = rcp_approx(s);
         const float rs2 = rs * rs;
         const float e1 = e * rs, t2 = tme * rs2;
-        const float reuse = fmaf(e1 + e1, rs2, tau * (tau - 2.0f));
+        const float reuse = fmaf(e1 + e1, rs2, fmaf(tau, -2.0f, tt));
         float fi = fmaf(a0, t2, ps * e1);
         fi = fmaf(a1, reuse, fi);
-        fi = fmaf(a2 * cub, rs2 * rs2 * (1.0f / 3.0f), fi);
+        fi = fmaf(a2 * cub3, rs2 * rs2, fi);
         tally.v[k] = weight * fi;
         float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);

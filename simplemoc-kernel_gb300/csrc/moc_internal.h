@@ -124,7 +124,7 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
 constexpr int RING_DEPTH = 8;  // depth of the shared-memory prefetch ring
 struct FwdConfig {
     int vec;              // groups per lane: 1, 2, 4
-    int warps_per_block;  // 1..8
+    int warps_per_block;  // 1..16
     int exp_kind;         // ExpKind
     int blocks;           // grid size (0 = fill the GPU)
     int store = STORE_F32;
@@ -139,6 +139,9 @@ size_t fwd_smem_bytes(const FwdConfig &cfg, int tab_n);
 // Default groups per lane for G groups (measured fastest at G = 64 and 128 on GB300:
 // two groups per lane keeps registers low enough for 32 resident warps per SM).
 inline int auto_vec(int G) { return G > 32 ? 2 : 1; }
+// Default warps per block: 8, or 16 in table mode, where each block stages the table in
+// shared memory (80 KB at 10,000 points): two blocks of 16 warps keep 32 warps per SM.
+inline int auto_warps_per_block(int exp_kind) { return exp_kind == EXPK_TABLE ? 16 : 8; }
 // Resident blocks per SM for a configuration (0 if the configuration is invalid).
 int fwd_blocks_per_sm(const FwdConfig &cfg, int tab_n);
 

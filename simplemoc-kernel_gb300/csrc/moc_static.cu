@@ -145,8 +145,9 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
 
     moc::FwdConfig cfg;
     cfg.vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
-    cfg.warps_per_block = o->warps_per_block ? o->warps_per_block : 8;
     cfg.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+    cfg.warps_per_block =
+        o->warps_per_block ? o->warps_per_block : moc::auto_warps_per_block(cfg.exp_kind);
     cfg.prefetch = o->prefetch > 1 ? o->prefetch : 1;
     const int per_sm = moc::fwd_blocks_per_sm(cfg, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;

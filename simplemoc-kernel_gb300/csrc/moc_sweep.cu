@@ -21,8 +21,9 @@
 //    (cell, ds) per segment; the next window is loaded 32 segments ahead;
 //  * the segment loop is unrolled by two with ping-pong registers: the block of segment
 //    j+1 is loaded before segment j is computed, without register moves; the pairs run
-//    inside each 32-segment window with 32-bit indices (table mode keeps a loop over the
-//    whole item, measured faster there).
+//    inside each 32-segment window with 32-bit indices;
+//  * segments are branch-free: past the item's end or with a bad index a segment is a
+//    null-cell no-op, idle lanes read group 0, the tally is one predicated reduction.
 // Tallies go out as red.global.add.v4.f32 (one L2 request per lane, 16 bytes).
 #include "moc_device.cuh"
 #include "moc_internal.h"
@@ -173,13 +174,14 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
         const float s = x.v[k].x, a0 = x.v[k].y, a1 = x.v[k].z, a2 = x.v[k].w;
         const float ps = psi.v[k];
         const float tau = __fmul_rn(s, ds);  // kept exact: the table index depends on it
-        float e, p, tme, cub;
+        const float tt = tau * tau;
+        float e, p, tme, cub3;                 // cub3 = (tau(tau(tau-3)+6) - 6e) / 3
         if constexpr (EK == EXPK_STABLE) {
             const ExpTerms x = exp_terms_stable(tau);
             e = x.e;
             p = x.p;
             tme = x.tme;
-            cub = x.cub;
+            cub3 = x.cub * (1.0f / 3.0f);
         } else {
             if constexpr (EK == EXPK_TABLE) {
                 e = table_lookup(tr.tab, tr.n, tr.dx, tr.max, tau);
@@ -189,18 +191,18 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
                 e = 1.0f - p;
             }
             tme = tau - e;
-            // tau(tau(tau-3)+6) - 6e = tau^2 (tau - 3) + 6 (tau - e)
-            cub = fmaf(tau * tau, tau - 3.0f, 6.0f * tme);
+            // (tau(tau(tau-3)+6) - 6e)/3 = tau^2 (tau/3 - 1) + 2 (tau - e)
+            cub3 = fmaf(tt, fmaf(tau, 1.0f / 3.0f, -1.0f), tme + tme);
         }
         // (q0 tau + (s psi - q0) e)/s^2 == q0 (tau - e)/s^2 + psi e/s exactly, so FI and
         // psi' share e/s and (tau - e)/s^2; 2e/s^3 = 2 (e/s) / s^2.
         const float rs = rcp_approx(s);
         const float rs2 = rs * rs;
         const float e1 = e * rs, t2 = tme * rs2;
-        const float reuse = fmaf(e1 + e1, rs2, tau * (tau - 2.0f));
+        const float reuse = fmaf(e1 + e1, rs2, fmaf(tau, -2.0f, tt));
         float fi = fmaf(a0, t2, ps * e1);
         fi = fmaf(a1, reuse, fi);
-        fi = fmaf(a2 * cub, rs2 * rs2 * (1.0f / 3.0f), fi);
+        fi = fmaf(a2 * cub3, rs2 * rs2, fi);
         tally.v[k] = weight * fi;
         float pn = fmaf(a1, t2, a0 * e1);
         pn = fmaf(a2, reuse, pn);
@@ -209,9 +211,9 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
     }
 }
 
-// Lane-parallel descriptor decode of segment j: its cell index (or -1 if the region or
-// interval is out of range, reported once through the error word) and its ds.
-// A segment past the item's end or with an out-of-range index decodes to cell `none`
+// Lane-parallel descriptor decode of segment j: its cell index and its ds. Out-of-range
+// regions or intervals are reported through the error word. A segment past the item's
+// end or with an out-of-range index decodes to cell `none`
 // with ds = 0: -1 (skipped by the loops that test it), or the null cell R*I, whose block
 // (sigT 1, coefficients 0) makes the segment an exact no-op (p = 1, every term 0).
 __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t end, int none,
@@ -491,7 +493,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
 // Dynamic shared memory: the exponential table (table mode), then one prefetch ring of
 // RD * VEC * 32 float4 per warp.
 template <int VEC, int EK, int ST, int TL, int RD, int MODE>
-__global__ void __launch_bounds__(256) fwd_kernel(const SweepParams P)
+__global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
 {
     extern __shared__ float4 s_dyn[];
     TableRef tr{nullptr, 0, 0.0f, 0.0f};
@@ -566,19 +568,14 @@ const void *fwd_fn()
     return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD, MODE>);
 }
 
-// The register-prefetch loop: the branch-free windowed pair loop (RD = -1) for the plain
-// and stable math where the configuration allows it (a null-cell row, G a multiple of
-// VEC), else the ping-pong loop with per-segment checks (RD = 0); table mode always takes
-// the ping-pong loop (measured faster there on GB300).
+// The register-prefetch loop: the branch-free windowed pair loop (RD = -1) where the
+// configuration allows it (a null-cell row, G a multiple of VEC), else the ping-pong loop
+// with per-segment checks (RD = 0).
 template <int VEC, int EK, int ST, int TL, int MODE = MODE_SWEEP>
 const void *reg_fn(bool branch_free)
 {
-    if constexpr (EK == EXPK_TABLE) {
-        return fwd_fn<VEC, EK, ST, TL, 0, MODE>();
-    } else {
-        return branch_free ? fwd_fn<VEC, EK, ST, TL, -1, MODE>()
-                           : fwd_fn<VEC, EK, ST, TL, 0, MODE>();
-    }
+    return branch_free ? fwd_fn<VEC, EK, ST, TL, -1, MODE>()
+                       : fwd_fn<VEC, EK, ST, TL, 0, MODE>();
 }
 
 // The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
@@ -712,7 +709,7 @@ size_t fwd_smem_bytes(const FwdConfig &c, int tab_n)
 int fwd_blocks_per_sm(const FwdConfig &c, int tab_n)
 {
     const void *fn = pick(c);
-    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 8) return 0;
+    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 16) return 0;
     const size_t smem = fwd_smem_bytes(c, tab_n);
     int n = 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -727,7 +724,7 @@ int fwd_blocks_per_sm(const FwdConfig &c, int tab_n)
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &c, cudaStream_t st)
 {
     const void *fn = pick(c);
-    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 8 || c.blocks < 1)
+    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 16 || c.blocks < 1)
         return cudaErrorInvalidValue;
     const size_t smem = fwd_smem_bytes(c, p.tab_n);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
