@@ -44,6 +44,8 @@ struct moc_handle_s {
     int2 *bqueue = nullptr;
     size_t bqueue_cap = 0;
     float *bsave = nullptr;    // autotuner: saved psi and fine_flux
+    unsigned char *bsplit = nullptr;  // batch: split workspace of every problem
+    size_t bsplit_cap = 0;
     size_t bsave_cap = 0;
     cudaStream_t gstream = nullptr;        // capture stream of the batch graph
     cudaGraphExec_t gexec = nullptr;
@@ -190,13 +192,15 @@ moc_status_t ensure_table(moc_handle_t h, const moc_fwd_opts_t *o, cudaStream_t 
 // SM): the sweep of S segments x n_gch group chunks takes S n_gch / 9e9 s. Tracks whose
 // lone time would exceed a quarter of that, L* = S n_gch / 9360 segments, are cut into
 // chunks of L* / 4 (rounded to a power of two, at least 32).
-int auto_chunk(int64_t S, int64_t n_gch)
+int auto_chunk_steps(double warp_steps)
 {
-    const double target = (double)S * (double)n_gch / 9360.0 / moc::SPLIT_MIN_FACTOR;
+    const double target = warp_steps / 9360.0 / moc::SPLIT_MIN_FACTOR;
     int c = 32;
     while (c < moc::SPLIT_CHUNK_MAX && c * 1.41421356 < target) c *= 2;
     return c;
 }
+
+int auto_chunk(int64_t S, int64_t n_gch) { return auto_chunk_steps((double)S * (double)n_gch); }
 
 // Whether long tracks are split (opts.track_chunk, and S long enough for any track to be
 // cut), and if so the split workspace, wired into *sp. Record and map counts share one
@@ -421,23 +425,63 @@ std::vector<unsigned char> set_key(const moc_problem_t *probs, int32_t n, const 
     std::vector<unsigned char> key;
     append(key, probs, sizeof(moc_problem_t) * (size_t)n);
     const float f[7] = {o->table_max, o->dz, o->zin, o->weight, o->mu, o->mu2, 0.0f};
-    const int32_t i[2] = {(int32_t)o->exp_mode, o->table_points};
+    const int32_t i[3] = {(int32_t)o->exp_mode, o->table_points, o->track_chunk};
     append(key, f, sizeof(f));
     append(key, i, sizeof(i));
     return key;
 }
 
+// Long-track split of each problem of a batch: its records, maps and starts are made by
+// the single-problem passes before the batched sweep, which then takes chunk records as
+// its units.
+struct BatchSplit {
+    bool on[MOC_BATCH_MAX_PROBLEMS] = {};
+    moc::SweepParams sp[MOC_BATCH_MAX_PROBLEMS];
+    moc::SplitWork sw[MOC_BATCH_MAX_PROBLEMS];
+    moc::FwdConfig mcfg[MOC_BATCH_MAX_PROBLEMS];
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
 // Lay out sub-problems, workspace and launch parameters for one (vec, wpb) choice.
 moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
                          const moc_fwd_opts_t *o, int vec, int wpb, moc::BatchParams &B,
-                         moc::BatchWork &W, int &blocks)
+                         moc::BatchWork &W, BatchSplit &X, int &blocks)
 {
     moc_status_t s;
     std::memset(&B, 0, sizeof(B));
-    size_t blk_total = 0, perm_total = 0;
+    X = BatchSplit{};
+    // chunk length: from the whole batch's warp-segment steps (a problem's group range
+    // runs as ceil(G / 32 vec) warp-wide parts, or one sub-warp part for small G)
+    const int gw = 32 * vec;
+    double steps = 0.0;
     for (int32_t k = 0; k < n; k++) {
-        blk_total += (size_t)probs[k].n_regions * probs[k].n_intervals * probs[k].group_stride;
-        perm_total += (size_t)probs[k].n_tracks;
+        const int full = probs[k].n_groups / gw, rest = probs[k].n_groups % gw;
+        double per_track = full;
+        if (rest) {
+            int lpt = 1;
+            while (lpt < (rest + vec - 1) / vec) lpt *= 2;
+            per_track += (double)lpt / 32.0;
+        }
+        steps += (double)probs[k].n_segments * per_track;
+    }
+    const int chunk_len = o->track_chunk == 0 ? auto_chunk_steps(steps) : o->track_chunk;
+    size_t blk_total = 0, perm_total = 0, split_bytes = 0;
+    int64_t cap[MOC_BATCH_MAX_PROBLEMS] = {};
+    for (int32_t k = 0; k < n; k++) {
+        const moc_problem_t &p = probs[k];
+        // each problem's cell blocks and its null-cell row
+        blk_total += ((size_t)p.n_regions * p.n_intervals + 1) * p.group_stride;
+        X.on[k] = o->track_chunk != -1 && p.n_tracks > 0 &&
+                  p.n_segments > (int64_t)moc::SPLIT_MIN_FACTOR * chunk_len &&
+                  moc::split_max_records(p.n_tracks, p.n_segments, chunk_len) < INT32_MAX;
+        cap[k] = X.on[k] ? moc::split_max_records(p.n_tracks, p.n_segments, chunk_len) : 0;
+        perm_total += X.on[k] ? (size_t)cap[k] : (size_t)p.n_tracks;
+        if (X.on[k]) {
+            const size_t T = p.n_tracks, Gs = p.group_stride, c = cap[k];
+            split_bytes += align_up((T + 1) * 8) + align_up((T + 1023) / 1024 * 8) +
+                           align_up(c * 16) + align_up((c + 1) * 8) + 3 * align_up(c * Gs * 4);
+        }
     }
     if ((s = ensure(h, reinterpret_cast<void **>(&h->bblk), &h->bblk_cap,
                     (blk_total ? blk_total : 1) * sizeof(float4))))
@@ -448,10 +492,19 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
     if ((s = ensure(h, reinterpret_cast<void **>(&h->bhist), &h->bhist_cap,
                     sizeof(int) * moc::BATCH_BUCKETS * (MOC_BATCH_MAX_PROBLEMS + 1))))
         return s;
-    size_t boff = 0;
+    if (split_bytes && (s = ensure(h, reinterpret_cast<void **>(&h->bsplit), &h->bsplit_cap,
+                                   split_bytes)))
+        return s;
+    if (o->exp_mode == MOC_EXP_TABLE) {
+        if ((s = ensure_table(h, o, h->hstream))) return s;
+        B.table = h->table;
+        B.tab_n = h->table_n;
+        B.tab_dx = h->table_dx;
+        B.tab_max = h->table_lookup;
+    }
+    size_t boff = 0, soff = 0;
     int perm_off = 0, nsub = 0;
     int64_t items = 0;
-    const int chunk = 32 * vec;
     for (int32_t k = 0; k < n; k++) {
         const moc_problem_t &p = probs[k];
         moc::BatchProb &bp = B.prob[k];
@@ -469,11 +522,85 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
         bp.T = p.n_tracks;
         bp.S = p.n_segments;
         bp.perm_off = perm_off;
-        boff += (size_t)p.n_regions * p.n_intervals * p.group_stride;
-        perm_off += p.n_tracks;
+        const int64_t ncell = (int64_t)p.n_regions * p.n_intervals;
+        boff += (size_t)(ncell + 1) * p.group_stride;
+        int64_t units = p.n_tracks;
+        if (X.on[k]) {
+            // the problem's split workspace and the parameters of its split passes
+            const size_t T = p.n_tracks, Gs = p.group_stride, c = cap[k];
+            unsigned char *base = h->bsplit + soff;
+            moc::SplitWork &sw = X.sw[k];
+            sw.base = reinterpret_cast<int64_t *>(base);
+            base += align_up((T + 1) * 8);
+            sw.bsum = reinterpret_cast<int64_t *>(base);
+            base += align_up((T + 1023) / 1024 * 8);
+            sw.rec = reinterpret_cast<int4 *>(base);
+            base += align_up(c * 16);
+            sw.map_list = reinterpret_cast<int64_t *>(base);
+            sw.n_map = sw.map_list + c;
+            base += align_up((c + 1) * 8);
+            float *start = reinterpret_cast<float *>(base);
+            base += align_up(c * Gs * 4);
+            float *map_a = reinterpret_cast<float *>(base);
+            base += align_up(c * Gs * 4);
+            float *map_b = reinterpret_cast<float *>(base);
+            base += align_up(c * Gs * 4);
+            soff = (size_t)(base - h->bsplit);
+            sw.cap = (int64_t)c;
+            sw.chunk = chunk_len;
+            sw.map_all = 0;
+            moc::SweepParams &sp = X.sp[k];
+            sp = moc::SweepParams{};
+            sp.R = p.n_regions;
+            sp.I = p.n_intervals;
+            sp.G = p.n_groups;
+            sp.Gs = p.group_stride;
+            sp.T = p.n_tracks;
+            sp.S = p.n_segments;
+            sp.off = p.track_offsets;
+            sp.reg = p.seg_region;
+            sp.itv = p.seg_interval;
+            sp.ds = p.seg_ds;
+            sp.blk = bp.blk;
+            sp.null_cell = (int32_t)ncell;
+            sp.group_major = 1;
+            sp.psi = p.psi;
+            sp.weight = o->weight;
+            sp.table = B.table;
+            sp.tab_n = B.tab_n;
+            sp.tab_dx = B.tab_dx;
+            sp.tab_max = B.tab_max;
+            sp.err = h->err;
+            sp.counter = h->counter + 1;  // unused by the map pass (static assignment)
+            sp.rec = sw.rec;
+            sp.n_rec = sw.base + T;
+            sp.map_list = sw.map_list;
+            sp.n_map = sw.n_map;
+            sp.rec_cap = (int64_t)c;
+            sp.start = start;
+            sp.map_a = map_a;
+            sp.map_b = map_b;
+            moc::FwdConfig &mc = X.mcfg[k];
+            mc.vec = moc::auto_vec(p.n_groups);
+            mc.warps_per_block = 8;
+            mc.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
+            mc.mode = 1;
+            mc.prefetch = 1;
+            mc.branch_free = p.n_groups % mc.vec == 0;
+            sp.n_chunks = (p.n_groups + 32 * mc.vec - 1) / (32 * mc.vec);
+            const int per_sm = moc::fwd_blocks_per_sm(mc, o->table_points);
+            if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+            mc.blocks = per_sm * h->sm_count;
+            bp.rec = sw.rec;
+            bp.n_rec = sw.base + T;
+            bp.start = start;
+            bp.rec_cap = (int64_t)c;
+            units = (int64_t)c;
+        }
+        perm_off += (int)units;
         // full chunks of 32*vec groups, then the remainder on narrower sub-warps
-        for (int g = 0; g < p.n_groups; g += chunk) {
-            const int count = p.n_groups - g < chunk ? p.n_groups - g : chunk;
+        for (int g = 0; g < p.n_groups; g += gw) {
+            const int count = p.n_groups - g < gw ? p.n_groups - g : gw;
             const int lanes = (count + vec - 1) / vec;
             int lpt = 1;
             while (lpt < lanes) lpt *= 2;
@@ -485,7 +612,7 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
             sb.lpt = lpt;
             sb.item_base = items;
             const int per_warp = 32 / lpt;
-            items += (p.n_tracks + per_warp - 1) / per_warp;
+            items += (units + per_warp - 1) / per_warp;
         }
     }
     B.n_prob = n;
@@ -494,13 +621,6 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
     B.weight = o->weight;
     B.err = h->err;
     B.counter = h->counter;
-    if (o->exp_mode == MOC_EXP_TABLE) {
-        if ((s = ensure_table(h, o, h->hstream))) return s;
-        B.table = h->table;
-        B.tab_n = h->table_n;
-        B.tab_dx = h->table_dx;
-        B.tab_max = h->table_lookup;
-    }
     if ((s = ensure(h, reinterpret_cast<void **>(&h->bqueue), &h->bqueue_cap,
                     (size_t)(items ? items : 1) * sizeof(int2))))
         return s;
@@ -519,15 +639,22 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
 // the sweep.
 moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
                            const moc_fwd_opts_t *o, const moc::BatchParams &B,
-                           const moc::BatchWork &W, int vec, int wpb, int blocks,
-                           cudaStream_t st)
+                           const moc::BatchWork &W, const BatchSplit &X, int vec, int wpb,
+                           int blocks, cudaStream_t st)
 {
     for (int32_t k = 0; k < n; k++)
         MOC_CUDA(h, moc::launch_prep_block(probs[k].sigT, probs[k].source,
                                            const_cast<float4 *>(B.prob[k].blk),
                                            probs[k].n_regions, probs[k].n_intervals,
                                            probs[k].group_stride, o->dz, o->zin, o->mu, o->mu2,
-                                           st));
+                                           st, true));
+    // long tracks: each problem's records, chunk maps and chunk starts
+    for (int32_t k = 0; k < n; k++) {
+        if (!X.on[k]) continue;
+        MOC_CUDA(h, moc::launch_split_records(X.sp[k], X.sw[k], st));
+        MOC_CUDA(h, moc::launch_fwd(X.sp[k], X.mcfg[k], st));
+        MOC_CUDA(h, moc::launch_split_start(X.sp[k], X.sw[k], st));
+    }
     if (B.n_items == 0) return MOC_OK;
     const int ek = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
     MOC_CUDA(h, moc::launch_batch(B, W, vec, ek, wpb, blocks, st));
@@ -623,6 +750,7 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->bperm) cudaFree(h->bperm);
     if (h->bqueue) cudaFree(h->bqueue);
     if (h->bsave) cudaFree(h->bsave);
+    if (h->bsplit) cudaFree(h->bsplit);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->gstream) cudaStreamDestroy(h->gstream);
     if (h->table) cudaFree(h->table);
@@ -664,8 +792,9 @@ moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs,
     if (!wpb) wpb = (h->tune_wpb && key == h->tune_key) ? h->tune_wpb : 8;
     moc::BatchParams B;
     moc::BatchWork W;
+    BatchSplit X;
     int blocks = 0;
-    if ((s = build_batch(h, probs, n, o, vec, wpb, B, W, blocks))) return s;
+    if ((s = build_batch(h, probs, n, o, vec, wpb, B, W, X, blocks))) return s;
     // the graph is valid for this set, this workspace and this launch shape
     append(key, &B, sizeof(B));
     append(key, &W, sizeof(W));
@@ -678,7 +807,7 @@ moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs,
         if (!h->gstream)
             MOC_CUDA(h, cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
         MOC_CUDA(h, cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeRelaxed));
-        s = enqueue_batch(h, probs, n, o, B, W, vec, wpb, blocks, h->gstream);
+        s = enqueue_batch(h, probs, n, o, B, W, X, vec, wpb, blocks, h->gstream);
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(h->gstream, &graph);
         if (s) {
@@ -704,7 +833,9 @@ moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs,
     MOC_CUDA(h, cudaGraphLaunch(h->gexec, st));
     if (prof) {
         MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
-        h->timed_launches = n + (B.n_items ? 7 : 0);
+        int cut = 0;
+        for (int32_t k = 0; k < n; k++) cut += X.on[k] ? 5 : 0;
+        h->timed_launches = n + cut + (B.n_items ? 7 : 0);
         h->timed_finish = false;
         h->timed_split = false;
     }
@@ -756,13 +887,14 @@ moc_status_t moc_autotune_batch(moc_handle_t h, const moc_problem_t *probs, int3
         for (int wi = 0; wi < 4 && s == MOC_OK; wi++) {
             moc::BatchParams B;
             moc::BatchWork W;
+            BatchSplit X;
             int blocks = 0;
-            if (build_batch(h, probs, n, o, vecs[vi], wpbs[wi], B, W, blocks)) continue;
+            if (build_batch(h, probs, n, o, vecs[vi], wpbs[wi], B, W, X, blocks)) continue;
             float best = 1e30f;
             for (int rep = 0; rep < 3 && s == MOC_OK; rep++) {
                 if ((s = copy_all(false))) break;
                 cudaEventRecord(a, st);
-                s = enqueue_batch(h, probs, n, o, B, W, vecs[vi], wpbs[wi], blocks, st);
+                s = enqueue_batch(h, probs, n, o, B, W, X, vecs[vi], wpbs[wi], blocks, st);
                 cudaEventRecord(b, st);
                 if (cudaEventSynchronize(b) != cudaSuccess) s = MOC_ERR_CUDA;
                 float ms = 0.0f;

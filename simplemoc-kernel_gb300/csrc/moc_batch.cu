@@ -29,20 +29,37 @@ __device__ __forceinline__ int len_bucket(int64_t len)
     return NB - 1 - k;
 }
 
-__device__ __forceinline__ int64_t track_len(const BatchParams &B, int p, int t)
+// Units of problem p: its tracks, or the chunk records of its tracks when long tracks are
+// cut (counted on the device; at most rec_cap).
+__device__ __forceinline__ int64_t units_of(const BatchProb &P)
 {
-    const int64_t *off = B.prob[p].off;
-    const int64_t a = off[t], b = off[t + 1];
+    if (!P.rec) return P.T;
+    const int64_t n = *P.n_rec;
+    return n < P.rec_cap ? n : P.rec_cap;
+}
+
+// Host-side upper bound on the units (grid sizes and item counts).
+__host__ __device__ __forceinline__ int64_t units_bound(const BatchProb &P)
+{
+    return P.rec ? P.rec_cap : P.T;
+}
+
+__device__ __forceinline__ int64_t track_len(const BatchParams &B, int p, int64_t u)
+{
+    const BatchProb &P = B.prob[p];
+    if (P.rec) return __ldg(P.rec + u).z & CHUNK_LEN_MASK;
+    const int64_t a = P.off[u], b = P.off[u + 1];
     return (b >= a) ? b - a : 0;
 }
 
-// 1. histogram of track-length buckets per problem
+// 1. histogram of unit-length buckets per problem
 __global__ void track_hist_kernel(const BatchParams B, int *hist)
 {
     for (int p = 0; p < B.n_prob; p++) {
-        const int T = B.prob[p].T;
-        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
-            atomicAdd(&hist[p * NB + len_bucket(track_len(B, p, t))], 1);
+        const int64_t n = units_of(B.prob[p]);
+        for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n;
+             u += (int64_t)gridDim.x * blockDim.x)
+            atomicAdd(&hist[p * NB + len_bucket(track_len(B, p, u))], 1);
     }
 }
 
@@ -59,14 +76,15 @@ __global__ void scan_rows_kernel(int *hist, int rows)
     }
 }
 
-// 3. scatter every track into its problem's sorted list
+// 3. scatter every unit into its problem's sorted list
 __global__ void track_scatter_kernel(const BatchParams B, int *cursor, int *perm)
 {
     for (int p = 0; p < B.n_prob; p++) {
-        const int T = B.prob[p].T;
-        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
-            const int pos = atomicAdd(&cursor[p * NB + len_bucket(track_len(B, p, t))], 1);
-            perm[B.prob[p].perm_off + pos] = t;
+        const int64_t n = units_of(B.prob[p]);
+        for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n;
+             u += (int64_t)gridDim.x * blockDim.x) {
+            const int pos = atomicAdd(&cursor[p * NB + len_bucket(track_len(B, p, u))], 1);
+            perm[B.prob[p].perm_off + pos] = (int)u;
         }
     }
 }
@@ -89,8 +107,12 @@ __global__ void item_hist_kernel(const BatchParams B, const int *perm, int *hist
         const int s = sub_of(B, it, local);
         const BatchSub &S = B.sub[s];
         const int first = (int)(local * (32 / S.lpt));
-        const int t = perm[B.prob[S.prob].perm_off + first];
-        atomicAdd(&hist[len_bucket(track_len(B, S.prob, t))], 1);
+        // items past the units counted on the device are empty: last bucket
+        const int bucket = first < units_of(B.prob[S.prob])
+                               ? len_bucket(track_len(B, S.prob,
+                                                      perm[B.prob[S.prob].perm_off + first]))
+                               : NB - 1;
+        atomicAdd(&hist[bucket], 1);
     }
 }
 
@@ -103,8 +125,11 @@ __global__ void item_scatter_kernel(const BatchParams B, const int *perm, int *c
         const int s = sub_of(B, it, local);
         const BatchSub &S = B.sub[s];
         const int first = (int)(local * (32 / S.lpt));
-        const int t = perm[B.prob[S.prob].perm_off + first];
-        const int pos = atomicAdd(&cursor[len_bucket(track_len(B, S.prob, t))], 1);
+        const int bucket = first < units_of(B.prob[S.prob])
+                               ? len_bucket(track_len(B, S.prob,
+                                                      perm[B.prob[S.prob].perm_off + first]))
+                               : NB - 1;
+        const int pos = atomicAdd(&cursor[bucket], 1);
         queue[pos] = make_int2(s, first);
     }
 }
@@ -168,14 +193,31 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchParams B, const i
         const int lpt = S.lpt;
         const int sw = lane / lpt, sl = lane - sw * lpt;
         const int pos = item.y + sw;
-        int t = -1;
-        if (pos < P.T && sw < 32 / lpt) t = perm[P.perm_off + pos];
+        int t = -1;  // this sub-warp's unit: a track, or a chunk record
+        if (pos < units_of(P) && sw < 32 / lpt) t = perm[P.perm_off + pos];
         const int g0 = S.g_begin + sl * VEC;
         const int nvalid = S.g_begin + S.g_count - g0;
         int64_t beg = 0, len = 0;
+        const float *psi_src = nullptr;
+        float *psi_dst = nullptr;  // null: a non-last chunk's outgoing psi is not kept
         if (t >= 0) {
-            beg = P.off[t];
-            const int64_t end = P.off[t + 1];
+            int64_t end;
+            int trk = t;
+            if (P.rec) {
+                const int4 r = __ldg(P.rec + t);
+                beg = (int64_t)(uint32_t)r.x | ((int64_t)r.y << 32);
+                end = beg + (r.z & CHUNK_LEN_MASK);
+                trk = r.w;
+                if ((unsigned)trk >= (unsigned)P.T) end = -1;  // reported below
+                const bool single = (r.z & CHUNK_SINGLE) != 0;
+                psi_src = single ? P.psi + (int64_t)trk * P.Gs : P.start + (int64_t)t * P.Gs;
+                psi_dst = (single || (r.z & CHUNK_LAST)) ? P.psi + (int64_t)trk * P.Gs
+                                                         : nullptr;
+            } else {
+                beg = P.off[t];
+                end = P.off[t + 1];
+                psi_src = psi_dst = P.psi + (int64_t)t * P.Gs;
+            }
             if (beg >= 0 && beg <= end && end <= P.S) {
                 len = end - beg;
             } else {
@@ -190,8 +232,7 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchParams B, const i
             maxlen = other > maxlen ? other : maxlen;
         }
         Vec<VEC> psi;
-        float *psi_row = P.psi + (int64_t)(t < 0 ? 0 : t) * P.Gs + g0;
-        if (act) psi = ld_psi<VEC>(psi_row, nvalid);
+        if (act) psi = ld_psi<VEC>(psi_src + g0, nvalid);
         const float4 *bb = P.blk + g0;
         int cw = -1;
         float dw = 0.0f;
@@ -222,7 +263,7 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchParams B, const i
                 red_row<VEC>(P.ff + c * P.Gs + g0, tally, nvalid);
             }
         }
-        if (act) st_psi<VEC>(psi_row, psi, nvalid);
+        if (act && psi_dst) st_psi<VEC>(psi_dst + g0, psi, nvalid);
     }
 }
 
@@ -269,7 +310,10 @@ cudaError_t launch_batch(const BatchParams &B, const BatchWork &W, int vec, int 
         return cudaErrorInvalidValue;
     cudaError_t e;
     int64_t max_t = 0;
-    for (int p = 0; p < B.n_prob; p++) max_t = B.prob[p].T > max_t ? B.prob[p].T : max_t;
+    for (int p = 0; p < B.n_prob; p++) {
+        const int64_t u = units_bound(B.prob[p]);
+        max_t = u > max_t ? u : max_t;
+    }
     // length-sorted track lists
     if ((e = cudaMemsetAsync(W.hist, 0, sizeof(int) * NB * (B.n_prob + 1), st))) return e;
     track_hist_kernel<<<grid_for(max_t), 256, 0, st>>>(B, W.hist);

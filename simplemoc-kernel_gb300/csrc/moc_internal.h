@@ -164,8 +164,15 @@ struct BatchProb {                   // one problem (device pointers)
     const float4 *blk;               // its cell blocks (FP32)
     float *ff;
     float *psi;
-    int32_t R, I, G, Gs, T, perm_off;  // perm_off: start of its sorted track list
+    int32_t R, I, G, Gs, T, perm_off;  // perm_off: start of its sorted unit list
     int64_t S;
+    // long tracks cut into chunks (rec != null): the units are chunk records (as in the
+    // single-problem sweep), rec_cap of them at most, n_rec on the device; a chunk of a
+    // cut track starts from start[record] and only a track's last chunk writes its psi
+    const int4 *rec;
+    const int64_t *n_rec;
+    const float *start;
+    int64_t rec_cap;
 };
 struct BatchSub {                    // one group range of one problem
     int32_t prob, g_begin, g_count, lpt;  // lpt: lanes per track (power of two <= 32)

@@ -38,21 +38,27 @@ def run_batch(handle, hps, opts=None):
     return dps, arr
 
 
-def test_batch_matches_oracle_and_single_calls(handle):
+@pytest.mark.parametrize("chunk", [0, -1, 64])
+def test_batch_matches_oracle_and_single_calls(handle, chunk):
+    """Each problem of the batch against the FP64 oracle, and against a single call that
+    cuts its tracks the same way (chunk -1: no cuts; 64: tracks of more than 256 segments
+    cut into 64-segment chunks; 0: the automatic length, from the whole batch's size in
+    the batch, so the single calls are compared only with the oracle)."""
     hps = problems(tracks=1500)
-    dps, _ = run_batch(handle, hps)
+    opts = mocatt.default_opts(track_chunk=chunk)
+    dps, _ = run_batch(handle, hps, opts)
     for hp, dp in zip(hps, dps):
         psi, ff = dp.to_host("psi"), dp.to_host("fine_flux")
         parity.check_plain(psi, ff, oracle.fwd_fp64(hp), hp.G)
-        # the batched sweep runs every track in one pass: compare with single calls that
-        # do the same
+        if hp.Gs > hp.G:
+            assert not ff[:, hp.G:].any()
+        if chunk == 0:
+            continue
         single = mocatt.DeviceProblem(hp)
-        handle.fwd(single, mocatt.default_opts(track_chunk=-1))
+        handle.fwd(single, opts)
         assert handle.synchronize() == 0
         d = np.abs(psi[:, :hp.G].astype(np.float64) - single.to_host("psi")[:, :hp.G])
         assert np.all(d <= 1e-6 * np.abs(psi[:, :hp.G]) + 1e-30)
-        if hp.Gs > hp.G:
-            assert not ff[:, hp.G:].any()
 
 
 def test_batch_full_size_and_graph_replay(handle):
