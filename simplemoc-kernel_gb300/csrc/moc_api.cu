@@ -46,6 +46,10 @@ struct moc_handle_s {
     float *bsave = nullptr;    // autotuner: saved psi and fine_flux
     unsigned char *bsplit = nullptr;  // batch: split workspace of every problem
     size_t bsplit_cap = 0;
+    // batch: one side stream per problem for its cell-block and split passes, forked from
+    // and joined back into the batch's stream (parallel branches of the captured graph)
+    cudaStream_t bside[MOC_BATCH_MAX_PROBLEMS] = {};
+    cudaEvent_t bfork = nullptr, bjoin[MOC_BATCH_MAX_PROBLEMS] = {};
     size_t bsave_cap = 0;
     cudaStream_t gstream = nullptr;        // capture stream of the batch graph
     cudaGraphExec_t gexec = nullptr;
@@ -642,18 +646,32 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
                            const moc::BatchWork &W, const BatchSplit &X, int vec, int wpb,
                            int blocks, cudaStream_t st)
 {
-    for (int32_t k = 0; k < n; k++)
+    // Per problem, on its own side stream: the cell blocks, then (long tracks) its
+    // records, chunk maps and chunk starts. The problems' passes are independent, and a
+    // map pass over a few long chunks is latency-bound, so they run side by side.
+    if (!h->bfork) MOC_CUDA(h, cudaEventCreateWithFlags(&h->bfork, cudaEventDisableTiming));
+    for (int32_t k = 0; k < n; k++) {
+        if (!h->bside[k])
+            MOC_CUDA(h, cudaStreamCreateWithFlags(&h->bside[k], cudaStreamNonBlocking));
+        if (!h->bjoin[k])
+            MOC_CUDA(h, cudaEventCreateWithFlags(&h->bjoin[k], cudaEventDisableTiming));
+    }
+    MOC_CUDA(h, cudaEventRecord(h->bfork, st));
+    for (int32_t k = 0; k < n; k++) {
+        cudaStream_t sk = h->bside[k];
+        MOC_CUDA(h, cudaStreamWaitEvent(sk, h->bfork, 0));
         MOC_CUDA(h, moc::launch_prep_block(probs[k].sigT, probs[k].source,
                                            const_cast<float4 *>(B.prob[k].blk),
                                            probs[k].n_regions, probs[k].n_intervals,
                                            probs[k].group_stride, o->dz, o->zin, o->mu, o->mu2,
-                                           st, true));
-    // long tracks: each problem's records, chunk maps and chunk starts
-    for (int32_t k = 0; k < n; k++) {
-        if (!X.on[k]) continue;
-        MOC_CUDA(h, moc::launch_split_records(X.sp[k], X.sw[k], st));
-        MOC_CUDA(h, moc::launch_fwd(X.sp[k], X.mcfg[k], st));
-        MOC_CUDA(h, moc::launch_split_start(X.sp[k], X.sw[k], st));
+                                           sk, true));
+        if (X.on[k]) {
+            MOC_CUDA(h, moc::launch_split_records(X.sp[k], X.sw[k], sk));
+            MOC_CUDA(h, moc::launch_fwd(X.sp[k], X.mcfg[k], sk));
+            MOC_CUDA(h, moc::launch_split_start(X.sp[k], X.sw[k], sk));
+        }
+        MOC_CUDA(h, cudaEventRecord(h->bjoin[k], sk));
+        MOC_CUDA(h, cudaStreamWaitEvent(st, h->bjoin[k], 0));
     }
     if (B.n_items == 0) return MOC_OK;
     const int ek = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
@@ -751,6 +769,11 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->bqueue) cudaFree(h->bqueue);
     if (h->bsave) cudaFree(h->bsave);
     if (h->bsplit) cudaFree(h->bsplit);
+    for (int k = 0; k < MOC_BATCH_MAX_PROBLEMS; k++) {
+        if (h->bside[k]) cudaStreamDestroy(h->bside[k]);
+        if (h->bjoin[k]) cudaEventDestroy(h->bjoin[k]);
+    }
+    if (h->bfork) cudaEventDestroy(h->bfork);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->gstream) cudaStreamDestroy(h->gstream);
     if (h->table) cudaFree(h->table);
