@@ -3,6 +3,7 @@
 #include "moc_attenuate.h"
 #include "moc_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -66,6 +67,9 @@ struct moc_handle_s {
     void *hbuf[8] = {};
     size_t hcap[8] = {};
     cudaStream_t hstream = nullptr;
+    // its pipeline: copies in, sweeps (hstream) and copies out overlap part by part
+    cudaStream_t hin = nullptr, hout = nullptr;
+    cudaEvent_t hev_tab = nullptr, hev_in[8] = {}, hev_done[8] = {};
     // kernel timing of the last profiled call
     cudaEvent_t ev[5] = {};   // start, after prep, after sweep, after finish, after split
     int timed_launches = 0;   // 0: no profiled call yet
@@ -286,8 +290,10 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
     return MOC_OK;
 }
 
+// The forward sweep of one problem on device buffers. prep = false: the cell blocks of
+// this problem's tables are already in h->blk (a later part of a pipelined call).
 moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
-                        cudaStream_t st)
+                        cudaStream_t st, bool prep = true)
 {
     moc_status_t s;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
@@ -367,11 +373,11 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (prof && !h->ev[0])
         for (auto &e : h->ev) MOC_CUDA(h, cudaEventCreate(&e));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
-    if (cfg.store == moc::STORE_F32)
+    if (prep && cfg.store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
                                            o->mu, o->mu2, st, true));
-    else
+    else if (prep)
         MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
                                              p->n_regions, p->n_intervals, p->group_stride,
                                              o->dz, o->zin, o->mu, o->mu2, st, true));
@@ -394,7 +400,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (finish) MOC_CUDA(h, moc::launch_finish(p->fine_flux, sp.lo, sp.ff64, (int64_t)nff, st));
     if (prof) {
         if (finish) MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
-        h->timed_launches = (finish ? 3 : 2) + (split ? 5 : 0);
+        h->timed_launches = (finish ? 3 : 2) + (split ? 5 : 0) - (prep ? 0 : 1);
         h->timed_finish = finish;
         h->timed_split = split;
     }
@@ -679,6 +685,96 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
     return MOC_OK;
 }
 
+// Pipelined host-buffer sweep: the tables go up first; the tracks are then cut into
+// `parts` contiguous ranges of about equal segment counts, and while part k sweeps on
+// hstream, part k+1's descriptors and psi go up on hin and part k-1's psi comes back on
+// hout. Parts share the cell blocks and add into the same fine_flux; the chunk length of
+// long tracks is fixed from the whole problem, so psi is the one-call result bit for bit.
+moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
+                                int parts, const int64_t *cut)
+{
+    moc_status_t s;
+    const int64_t T = p->n_tracks, S = p->n_segments, Gs = p->group_stride;
+    const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
+    if (!h->hin) MOC_CUDA(h, cudaStreamCreateWithFlags(&h->hin, cudaStreamNonBlocking));
+    if (!h->hout) MOC_CUDA(h, cudaStreamCreateWithFlags(&h->hout, cudaStreamNonBlocking));
+    if (!h->hev_tab) MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_tab, cudaEventDisableTiming));
+    for (int k = 0; k < parts; k++) {
+        if (!h->hev_in[k])
+            MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_in[k], cudaEventDisableTiming));
+        if (!h->hev_done[k])
+            MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_done[k], cudaEventDisableTiming));
+    }
+    int64_t *d_off = static_cast<int64_t *>(h->hbuf[0]);
+    int32_t *d_reg = static_cast<int32_t *>(h->hbuf[1]);
+    uint8_t *d_itv = static_cast<uint8_t *>(h->hbuf[2]);
+    float *d_ds = static_cast<float *>(h->hbuf[3]);
+    float *d_sig = static_cast<float *>(h->hbuf[4]);
+    float *d_src = static_cast<float *>(h->hbuf[5]);
+    float *d_ff = static_cast<float *>(h->hbuf[6]);
+    float *d_psi = static_cast<float *>(h->hbuf[7]);
+    cudaStream_t cin = h->hin, comp = h->hstream, cout = h->hout;
+    // tables, offsets and the tallies first
+    MOC_CUDA(h, cudaMemcpyAsync(d_off, p->track_offsets, (size_t)(T + 1) * 8,
+                                cudaMemcpyHostToDevice, cin));
+    MOC_CUDA(h, cudaMemcpyAsync(d_sig, p->sigT, (size_t)p->n_regions * Gs * 4,
+                                cudaMemcpyHostToDevice, cin));
+    MOC_CUDA(h, cudaMemcpyAsync(d_src, p->source, (size_t)ncell * Gs * 4,
+                                cudaMemcpyHostToDevice, cin));
+    MOC_CUDA(h, cudaMemcpyAsync(d_ff, p->fine_flux, (size_t)ncell * Gs * 4,
+                                cudaMemcpyHostToDevice, cin));
+    MOC_CUDA(h, cudaEventRecord(h->hev_tab, cin));
+    MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), comp));
+    MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_tab, 0));
+    moc_problem_t d = *p;
+    d.track_offsets = d_off;
+    d.seg_region = d_reg;
+    d.seg_interval = d_itv;
+    d.seg_ds = d_ds;
+    d.sigT = d_sig;
+    d.source = d_src;
+    d.fine_flux = d_ff;
+    d.psi = d_psi;
+    moc_fwd_opts_t oo = *o;
+    if (oo.track_chunk == 0) {
+        const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
+        oo.track_chunk = auto_chunk(S, (p->n_groups + 32 * vec - 1) / (32 * vec));
+    }
+    for (int k = 0; k < parts; k++) {
+        const int64_t t0 = cut[k], t1 = cut[k + 1];
+        const int64_t s0 = p->track_offsets[t0], s1 = p->track_offsets[t1];
+        if (s1 > s0) {
+            MOC_CUDA(h, cudaMemcpyAsync(d_reg + s0, p->seg_region + s0, (size_t)(s1 - s0) * 4,
+                                        cudaMemcpyHostToDevice, cin));
+            MOC_CUDA(h, cudaMemcpyAsync(d_itv + s0, p->seg_interval + s0, (size_t)(s1 - s0),
+                                        cudaMemcpyHostToDevice, cin));
+            MOC_CUDA(h, cudaMemcpyAsync(d_ds + s0, p->seg_ds + s0, (size_t)(s1 - s0) * 4,
+                                        cudaMemcpyHostToDevice, cin));
+        }
+        MOC_CUDA(h, cudaMemcpyAsync(d_psi + t0 * Gs, p->psi + t0 * Gs,
+                                    (size_t)(t1 - t0) * Gs * 4, cudaMemcpyHostToDevice, cin));
+        MOC_CUDA(h, cudaEventRecord(h->hev_in[k], cin));
+        MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_in[k], 0));
+        // part k: its tracks, absolute segment offsets into the full descriptor arrays
+        moc_problem_t part = d;
+        part.track_offsets = d_off + t0;
+        part.n_tracks = (int32_t)(t1 - t0);
+        part.psi = d_psi + t0 * Gs;
+        if ((s = fwd_device(h, &part, &oo, comp, k == 0))) return s;
+        MOC_CUDA(h, cudaEventRecord(h->hev_done[k], comp));
+        MOC_CUDA(h, cudaStreamWaitEvent(cout, h->hev_done[k], 0));
+        MOC_CUDA(h, cudaMemcpyAsync(p->psi + t0 * Gs, d_psi + t0 * Gs,
+                                    (size_t)(t1 - t0) * Gs * 4, cudaMemcpyDeviceToHost, cout));
+    }
+    MOC_CUDA(h, cudaMemcpyAsync(p->fine_flux, d_ff, (size_t)ncell * Gs * 4,
+                                cudaMemcpyDeviceToHost, cout));
+    MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                cout));
+    MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), cout));  // reported here
+    MOC_CUDA(h, cudaStreamSynchronize(cout));
+    return *h->err_host ? MOC_ERR_BAD_INDEX : MOC_OK;
+}
+
 }  // namespace
 
 // Argument checks shared with the other entry points (declared in moc_internal.h).
@@ -782,6 +878,13 @@ moc_status_t moc_destroy(moc_handle_t h)
     for (int k = 0; k < 8; k++)
         if (h->hbuf[k]) cudaFree(h->hbuf[k]);
     if (h->hstream) cudaStreamDestroy(h->hstream);
+    if (h->hin) cudaStreamDestroy(h->hin);
+    if (h->hout) cudaStreamDestroy(h->hout);
+    if (h->hev_tab) cudaEventDestroy(h->hev_tab);
+    for (int k = 0; k < 8; k++) {
+        if (h->hev_in[k]) cudaEventDestroy(h->hev_in[k]);
+        if (h->hev_done[k]) cudaEventDestroy(h->hev_done[k]);
+    }
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -1115,6 +1218,30 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
                           p->sigT, p->source, p->fine_flux, p->psi};
     for (int k = 0; k < 8; k++)
         if ((s = ensure(h, &h->hbuf[k], &h->hcap[k], bytes[k] ? bytes[k] : 16))) return s;
+    // Large problems whose offsets partition [0, S] take the pipelined path (parts of
+    // about 4M segments, at most 8); checked mode and small problems copy everything first.
+    const int parts = (int)std::min<int64_t>(8, std::max<int64_t>(1, S / (4 << 20)));
+    if (!o->checked && parts > 1 && T >= parts) {
+        bool csr = p->track_offsets[0] == 0 && p->track_offsets[T] == S;
+        for (int64_t t = 0; csr && t < T; t++) csr = p->track_offsets[t] <= p->track_offsets[t + 1];
+        if (csr) {
+            int64_t cut[9];
+            cut[0] = 0;
+            for (int k = 1; k < parts; k++) {
+                // first track whose start reaches k/parts of the segments
+                const int64_t target = S / parts * k;
+                int64_t lo = cut[k - 1], hi = T;
+                while (lo < hi) {
+                    const int64_t mid = (lo + hi) / 2;
+                    if (p->track_offsets[mid] < target) lo = mid + 1;
+                    else hi = mid;
+                }
+                cut[k] = lo;
+            }
+            cut[parts] = T;
+            return fwd_host_pipelined(h, p, o, parts, cut);
+        }
+    }
     cudaStream_t st = h->hstream;
     for (int k = 0; k < 8; k++)
         if (bytes[k])
@@ -1135,9 +1262,12 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
     if (bytes[7])
         MOC_CUDA(h, cudaMemcpyAsync(p->psi, d.psi, bytes[7], cudaMemcpyDeviceToHost, st));
     MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));  // reported here
     MOC_CUDA(h, cudaStreamSynchronize(st));
     return *h->err_host ? MOC_ERR_BAD_INDEX : MOC_OK;
 }
+
+
 
 moc_status_t moc_synchronize(moc_handle_t h, void *stream)
 {

@@ -133,6 +133,32 @@ def test_host_entry_point_matches_device(handle):
     parity.check_plain(psi_d, ff_d, ref, hp.G)
 
 
+@pytest.mark.parametrize("name,kw", [
+    ("sweep_50M_g128", dict(segments=9_000_000, tracks=20_000, regions=2_000, groups=64)),
+    ("adjoint_2M_g64", dict(tracks=30_000)),
+])
+def test_pipelined_host_entry_point(handle, name, kw):
+    """Above 8M segments the host-buffer entry point copies and sweeps in parts (tracks cut
+    into ranges of ~4M segments, copies overlapping the sweep): psi equals the device
+    entry point bit for bit (the long-track chunk length is the whole problem's), and both
+    outputs are inside the FP64 tolerance. The lognormal case cuts long tracks."""
+    hp = mocatt.generate(mocatt.WORKLOADS[name].with_(**kw))
+    assert hp.S > 8 * 2**20
+    psi_d, ff_d = run_gpu(handle, hp)
+    q = hp.copy()
+    handle.fwd_host(q)
+    assert np.array_equal(q.psi, psi_d)
+    ref = oracle.fwd_fp64(hp)
+    parity.check_plain(q.psi, q.fine_flux, ref, hp.G)
+    parity.check_plain(psi_d, ff_d, ref, hp.G)
+    # a bad segment in the last part is reported
+    bad = hp.copy()
+    bad.seg_region[hp.S - 3] = hp.R + 1
+    with pytest.raises(mocatt.MocError):
+        handle.fwd_host(bad)
+    assert handle.synchronize() == 0
+
+
 def test_bad_index_is_skipped_and_reported(handle):
     """A segment with an out-of-range region is skipped by the kernel's own bounds check
     and reported; checked mode rejects the problem before touching anything."""
