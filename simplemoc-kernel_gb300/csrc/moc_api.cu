@@ -64,8 +64,8 @@ struct moc_handle_s {
     unsigned long long *counter = nullptr;
     int32_t *err_host = nullptr;         // pinned mirror
     // device copies for the host-buffer entry point
-    void *hbuf[8] = {};
-    size_t hcap[8] = {};
+    void *hbuf[9] = {};        // [8]: the caller's fine_flux, added after the pipelined sweep
+    size_t hcap[9] = {};
     cudaStream_t hstream = nullptr;
     // its pipeline: copies in, sweeps (hstream) and copies out overlap part by part
     cudaStream_t hin = nullptr, hout = nullptr;
@@ -691,7 +691,7 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
 // hout. Parts share the cell blocks and add into the same fine_flux; the chunk length of
 // long tracks is fixed from the whole problem, so psi is the one-call result bit for bit.
 moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
-                                int parts, const int64_t *cut)
+                                int parts, const int64_t *cut, int64_t longest)
 {
     moc_status_t s;
     const int64_t T = p->n_tracks, S = p->n_segments, Gs = p->group_stride;
@@ -721,9 +721,10 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
                                 cudaMemcpyHostToDevice, cin));
     MOC_CUDA(h, cudaMemcpyAsync(d_src, p->source, (size_t)ncell * Gs * 4,
                                 cudaMemcpyHostToDevice, cin));
-    MOC_CUDA(h, cudaMemcpyAsync(d_ff, p->fine_flux, (size_t)ncell * Gs * 4,
-                                cudaMemcpyHostToDevice, cin));
     MOC_CUDA(h, cudaEventRecord(h->hev_tab, cin));
+    // the parts add their tallies into zeros; the caller's fine_flux goes up last and is
+    // added on the device before the copy back
+    MOC_CUDA(h, cudaMemsetAsync(d_ff, 0, (size_t)ncell * Gs * 4, comp));
     MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), comp));
     MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_tab, 0));
     moc_problem_t d = *p;
@@ -740,6 +741,10 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
         const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
         oo.track_chunk = auto_chunk(S, (p->n_groups + 32 * vec - 1) / (32 * vec));
     }
+    // no track long enough to be cut (the host has the offsets): the parts skip the split
+    // passes, with the same result
+    if (oo.track_chunk > 0 && longest <= (int64_t)moc::SPLIT_MIN_FACTOR * oo.track_chunk)
+        oo.track_chunk = -1;
     for (int k = 0; k < parts; k++) {
         const int64_t t0 = cut[k], t1 = cut[k + 1];
         const int64_t s0 = p->track_offsets[t0], s1 = p->track_offsets[t1];
@@ -766,6 +771,14 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
         MOC_CUDA(h, cudaMemcpyAsync(p->psi + t0 * Gs, d_psi + t0 * Gs,
                                     (size_t)(t1 - t0) * Gs * 4, cudaMemcpyDeviceToHost, cout));
     }
+    float *d_ff0 = static_cast<float *>(h->hbuf[8]);
+    MOC_CUDA(h, cudaMemcpyAsync(d_ff0, p->fine_flux, (size_t)ncell * Gs * 4,
+                                cudaMemcpyHostToDevice, cin));
+    MOC_CUDA(h, cudaEventRecord(h->hev_tab, cin));
+    MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_tab, 0));
+    MOC_CUDA(h, moc::launch_finish(d_ff, d_ff0, nullptr, ncell * Gs, comp));
+    MOC_CUDA(h, cudaEventRecord(h->hev_done[0], comp));
+    MOC_CUDA(h, cudaStreamWaitEvent(cout, h->hev_done[0], 0));
     MOC_CUDA(h, cudaMemcpyAsync(p->fine_flux, d_ff, (size_t)ncell * Gs * 4,
                                 cudaMemcpyDeviceToHost, cout));
     MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost,
@@ -875,7 +888,7 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->table) cudaFree(h->table);
     if (h->err) cudaFree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
-    for (int k = 0; k < 8; k++)
+    for (int k = 0; k < 9; k++)
         if (h->hbuf[k]) cudaFree(h->hbuf[k]);
     if (h->hstream) cudaStreamDestroy(h->hstream);
     if (h->hin) cudaStreamDestroy(h->hin);
@@ -1219,17 +1232,27 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
     for (int k = 0; k < 8; k++)
         if ((s = ensure(h, &h->hbuf[k], &h->hcap[k], bytes[k] ? bytes[k] : 16))) return s;
     // Large problems whose offsets partition [0, S] take the pipelined path (parts of
-    // about 4M segments, at most 8); checked mode and small problems copy everything first.
-    const int parts = (int)std::min<int64_t>(8, std::max<int64_t>(1, S / (4 << 20)));
+    // about 8M segments, at most 8, measured best on GB300 at 50M x 128 against 2M and 4M;
+    // the first part is half the others, so the first sweep starts sooner); checked mode
+    // and smaller problems copy everything first.
+    const int parts = (int)std::min<int64_t>(8, std::max<int64_t>(1, S / (8 << 20)));
     if (!o->checked && parts > 1 && T >= parts) {
         bool csr = p->track_offsets[0] == 0 && p->track_offsets[T] == S;
-        for (int64_t t = 0; csr && t < T; t++) csr = p->track_offsets[t] <= p->track_offsets[t + 1];
+        int64_t longest = 0;
+        for (int64_t t = 0; csr && t < T; t++) {
+            const int64_t len = p->track_offsets[t + 1] - p->track_offsets[t];
+            csr = len >= 0;
+            longest = len > longest ? len : longest;
+        }
+        if (csr && (s = ensure(h, &h->hbuf[8], &h->hcap[8], bytes[6] ? bytes[6] : 16)))
+            return s;
         if (csr) {
             int64_t cut[9];
             cut[0] = 0;
             for (int k = 1; k < parts; k++) {
-                // first track whose start reaches k/parts of the segments
-                const int64_t target = S / parts * k;
+                // first track whose start reaches (k - 1/2)/(parts - 1/2) of the segments
+                const int64_t target =
+                    (int64_t)((double)S * (2.0 * k - 1.0) / (2.0 * parts - 1.0));
                 int64_t lo = cut[k - 1], hi = T;
                 while (lo < hi) {
                     const int64_t mid = (lo + hi) / 2;
@@ -1239,7 +1262,7 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
                 cut[k] = lo;
             }
             cut[parts] = T;
-            return fwd_host_pipelined(h, p, o, parts, cut);
+            return fwd_host_pipelined(h, p, o, parts, cut, longest);
         }
     }
     cudaStream_t st = h->hstream;

@@ -156,21 +156,29 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
     if (dropped) atomicOr(P.err, DEVERR_OFFSETS);
 }
 
-// psi entering each chunk of every split track: one warp per track, lanes over groups.
+// psi entering each chunk of every split track. The map list holds every non-last chunk,
+// so each split track's first chunk appears in it once: one warp per map item, and the
+// warp whose item is a first chunk walks that track with its lanes over groups (an empty
+// list - no cut track - costs one load per warp).
 __global__ void split_start_kernel(const SweepParams P, const SplitWork W)
 {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < P.T;
-         t += nwarps) {
-        const int64_t b = W.base[t];
-        if (b >= W.cap) continue;
+    const float *__restrict__ ma = P.map_a;
+    const float *__restrict__ mb = P.map_b;
+    float *__restrict__ start = P.start;
+    int64_t n_map = *W.n_map;
+    n_map = n_map < W.cap ? n_map : W.cap;
+    for (int64_t m = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; m < n_map;
+         m += nwarps) {
+        const int64_t q = W.map_list[m];
+        if ((uint64_t)q >= (uint64_t)W.cap) continue;
+        const int4 r = W.rec[q];
+        if (!(r.z & CHUNK_FIRST) || (unsigned)r.w >= (unsigned)P.T) continue;
+        const int64_t t = r.w;
+        const int64_t b = q;
         const int64_t e = W.base[t + 1] < W.cap ? W.base[t + 1] : W.cap;
         const int64_t nq = e - b;
-        if (nq < 2) continue;
-        const float *__restrict__ ma = P.map_a;
-        const float *__restrict__ mb = P.map_b;
-        float *__restrict__ start = P.start;
         for (int g = lane; g < P.G; g += 32) {
             float psi = P.psi[t * P.Gs + g];
             // the maps of 8 chunks are loaded before their 8 dependent FMAs, so the chain
@@ -219,7 +227,7 @@ cudaError_t launch_split_records(const SweepParams &P, const SplitWork &W, cudaS
 
 cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStream_t st)
 {
-    split_start_kernel<<<grid_for((int64_t)P.T * 32), 256, 0, st>>>(P, W);
+    split_start_kernel<<<152 * 8, 256, 0, st>>>(P, W);
     return cudaGetLastError();
 }
 

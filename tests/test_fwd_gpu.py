@@ -134,16 +134,16 @@ def test_host_entry_point_matches_device(handle):
 
 
 @pytest.mark.parametrize("name,kw", [
-    ("sweep_50M_g128", dict(segments=9_000_000, tracks=20_000, regions=2_000, groups=64)),
-    ("adjoint_2M_g64", dict(tracks=30_000)),
+    ("sweep_50M_g128", dict(segments=18_000_000, tracks=40_000, regions=2_000, groups=64)),
+    ("adjoint_2M_g64", dict(tracks=50_000)),
 ])
 def test_pipelined_host_entry_point(handle, name, kw):
-    """Above 8M segments the host-buffer entry point copies and sweeps in parts (tracks cut
-    into ranges of ~4M segments, copies overlapping the sweep): psi equals the device
+    """From 16M segments on the host-buffer entry point copies and sweeps in parts (tracks
+    cut into ranges of ~8M segments, copies overlapping the sweeps): psi equals the device
     entry point bit for bit (the long-track chunk length is the whole problem's), and both
     outputs are inside the FP64 tolerance. The lognormal case cuts long tracks."""
     hp = mocatt.generate(mocatt.WORKLOADS[name].with_(**kw))
-    assert hp.S > 8 * 2**20
+    assert hp.S >= 2 * 8 * 2**20
     psi_d, ff_d = run_gpu(handle, hp)
     q = hp.copy()
     handle.fwd_host(q)
