@@ -68,8 +68,8 @@ struct moc_handle_s {
     size_t hcap[9] = {};
     cudaStream_t hstream = nullptr;
     // its pipeline: copies in, sweeps (hstream) and copies out overlap part by part
-    cudaStream_t hin = nullptr, hout = nullptr;
-    cudaEvent_t hev_tab = nullptr, hev_in[8] = {}, hev_done[8] = {};
+    cudaStream_t hin = nullptr, hout = nullptr, hcomp2 = nullptr;
+    cudaEvent_t hev_tab = nullptr, hev_prep = nullptr, hev_in[8] = {}, hev_done[8] = {};
     // kernel timing of the last profiled call
     cudaEvent_t ev[5] = {};   // start, after prep, after sweep, after finish, after split
     int timed_launches = 0;   // 0: no profiled call yet
@@ -293,8 +293,12 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
 // The forward sweep of one problem on device buffers. prep = false: the cell blocks of
 // this problem's tables are already in h->blk (a later part of a pipelined call).
 moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
-                        cudaStream_t st, bool prep = true)
+                        cudaStream_t st, bool prep = true,
+                        unsigned long long *counter = nullptr)
 {
+    // queue heads: [0] the sweep's, [1] the map pass's (a pipelined call gives every other
+    // part its own pair so that parts on two streams can overlap)
+    unsigned long long *ctr = counter ? counter : h->counter;
     moc_status_t s;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
     // cell blocks and the null-cell row after them
@@ -322,7 +326,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     sp.tab_dx = h->table_dx;
     sp.tab_max = h->table_lookup;
     sp.err = h->err;
-    sp.counter = h->counter;
+    sp.counter = ctr;
 
     if (o->checked) {
         MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));
@@ -384,12 +388,12 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (sp.lo) MOC_CUDA(h, cudaMemsetAsync(sp.lo, 0, nff * sizeof(float), st));
     if (sp.ff64) MOC_CUDA(h, cudaMemsetAsync(sp.ff64, 0, nff * sizeof(double), st));
     // counter[0]: the sweep's queue head, counter[1]: the map pass's
-    MOC_CUDA(h, cudaMemsetAsync(h->counter, 0, 2 * sizeof(unsigned long long), st));
+    MOC_CUDA(h, cudaMemsetAsync(ctr, 0, 2 * sizeof(unsigned long long), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     if (split) {
         MOC_CUDA(h, moc::launch_split_records(sp, sw, st));
         moc::SweepParams mp = sp;
-        mp.counter = h->counter + 1;
+        mp.counter = ctr + 1;
         MOC_CUDA(h, moc::launch_fwd(mp, mcfg, st));
         MOC_CUDA(h, moc::launch_split_start(sp, sw, st));
     }
@@ -685,6 +689,30 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
     return MOC_OK;
 }
 
+// The cell blocks (and the null-cell row) of a problem's tables, in the storage of its
+// precision form.
+moc_status_t prep_blocks(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
+                         cudaStream_t st)
+{
+    moc_status_t s;
+    const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
+    const size_t blk_bytes = (size_t)(ncell + 1) * p->group_stride * sizeof(float4);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, blk_bytes))) return s;
+    if (o->exp_mode == MOC_EXP_TABLE && (s = ensure_table(h, o, st))) return s;
+    const int store = o->precision == MOC_PREC_BF16   ? moc::STORE_BF16
+                      : o->precision == MOC_PREC_FP16 ? moc::STORE_F16
+                                                      : moc::STORE_F32;
+    if (store == moc::STORE_F32)
+        MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
+                                           p->n_intervals, p->group_stride, o->dz, o->zin,
+                                           o->mu, o->mu2, st, true));
+    else
+        MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, store, p->n_regions,
+                                             p->n_intervals, p->group_stride, o->dz, o->zin,
+                                             o->mu, o->mu2, st, true));
+    return MOC_OK;
+}
+
 // Pipelined host-buffer sweep: the tables go up first; the tracks are then cut into
 // `parts` contiguous ranges of about equal segment counts, and while part k sweeps on
 // hstream, part k+1's descriptors and psi go up on hin and part k-1's psi comes back on
@@ -698,7 +726,10 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
     if (!h->hin) MOC_CUDA(h, cudaStreamCreateWithFlags(&h->hin, cudaStreamNonBlocking));
     if (!h->hout) MOC_CUDA(h, cudaStreamCreateWithFlags(&h->hout, cudaStreamNonBlocking));
+    if (!h->hcomp2) MOC_CUDA(h, cudaStreamCreateWithFlags(&h->hcomp2, cudaStreamNonBlocking));
     if (!h->hev_tab) MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_tab, cudaEventDisableTiming));
+    if (!h->hev_prep)
+        MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_prep, cudaEventDisableTiming));
     for (int k = 0; k < parts; k++) {
         if (!h->hev_in[k])
             MOC_CUDA(h, cudaEventCreateWithFlags(&h->hev_in[k], cudaEventDisableTiming));
@@ -745,6 +776,15 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
     // passes, with the same result
     if (oo.track_chunk > 0 && longest <= (int64_t)moc::SPLIT_MIN_FACTOR * oo.track_chunk)
         oo.track_chunk = -1;
+    // Without split passes the parts share only read-only cell blocks and atomic tallies:
+    // consecutive parts alternate between two compute streams with their own queue heads,
+    // so a part's blocks fill the SMs its predecessor's tail leaves idle. With split passes
+    // (one split workspace) every part runs on one stream.
+    const bool two = oo.track_chunk == -1;
+    cudaStream_t cs[2] = {comp, two ? h->hcomp2 : comp};
+    if ((s = prep_blocks(h, &d, &oo, comp))) return s;
+    MOC_CUDA(h, cudaEventRecord(h->hev_prep, comp));
+    if (two) MOC_CUDA(h, cudaStreamWaitEvent(cs[1], h->hev_prep, 0));
     for (int k = 0; k < parts; k++) {
         const int64_t t0 = cut[k], t1 = cut[k + 1];
         const int64_t s0 = p->track_offsets[t0], s1 = p->track_offsets[t1];
@@ -759,14 +799,15 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
         MOC_CUDA(h, cudaMemcpyAsync(d_psi + t0 * Gs, p->psi + t0 * Gs,
                                     (size_t)(t1 - t0) * Gs * 4, cudaMemcpyHostToDevice, cin));
         MOC_CUDA(h, cudaEventRecord(h->hev_in[k], cin));
-        MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_in[k], 0));
+        cudaStream_t ck = cs[k & 1];
+        MOC_CUDA(h, cudaStreamWaitEvent(ck, h->hev_in[k], 0));
         // part k: its tracks, absolute segment offsets into the full descriptor arrays
         moc_problem_t part = d;
         part.track_offsets = d_off + t0;
         part.n_tracks = (int32_t)(t1 - t0);
         part.psi = d_psi + t0 * Gs;
-        if ((s = fwd_device(h, &part, &oo, comp, k == 0))) return s;
-        MOC_CUDA(h, cudaEventRecord(h->hev_done[k], comp));
+        if ((s = fwd_device(h, &part, &oo, ck, false, h->counter + 2 * (k & 1)))) return s;
+        MOC_CUDA(h, cudaEventRecord(h->hev_done[k], ck));
         MOC_CUDA(h, cudaStreamWaitEvent(cout, h->hev_done[k], 0));
         MOC_CUDA(h, cudaMemcpyAsync(p->psi + t0 * Gs, d_psi + t0 * Gs,
                                     (size_t)(t1 - t0) * Gs * 4, cudaMemcpyDeviceToHost, cout));
@@ -776,6 +817,11 @@ moc_status_t fwd_host_pipelined(moc_handle_t h, const moc_problem_t *p, const mo
                                 cudaMemcpyHostToDevice, cin));
     MOC_CUDA(h, cudaEventRecord(h->hev_tab, cin));
     MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_tab, 0));
+    if (two && parts > 1) {
+        // the second stream's last part (the odd one nearest the end)
+        const int last_odd = (parts - 1) % 2 == 1 ? parts - 1 : parts - 2;
+        MOC_CUDA(h, cudaStreamWaitEvent(comp, h->hev_done[last_odd], 0));
+    }
     MOC_CUDA(h, moc::launch_finish(d_ff, d_ff0, nullptr, ncell * Gs, comp));
     MOC_CUDA(h, cudaEventRecord(h->hev_done[0], comp));
     MOC_CUDA(h, cudaStreamWaitEvent(cout, h->hev_done[0], 0));
@@ -893,7 +939,9 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->hstream) cudaStreamDestroy(h->hstream);
     if (h->hin) cudaStreamDestroy(h->hin);
     if (h->hout) cudaStreamDestroy(h->hout);
+    if (h->hcomp2) cudaStreamDestroy(h->hcomp2);
     if (h->hev_tab) cudaEventDestroy(h->hev_tab);
+    if (h->hev_prep) cudaEventDestroy(h->hev_prep);
     for (int k = 0; k < 8; k++) {
         if (h->hev_in[k]) cudaEventDestroy(h->hev_in[k]);
         if (h->hev_done[k]) cudaEventDestroy(h->hev_done[k]);
