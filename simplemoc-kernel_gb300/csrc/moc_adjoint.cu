@@ -42,11 +42,16 @@ struct AdjTerms {
 __device__ __forceinline__ AdjTerms adj_terms(float tau)
 {
     AdjTerms r;
-    if (tau < 1.0f) {
+    if (tau < 2.0f) {
         // s4 = sum_{k>=4} (-1)^k tau^k / k! = tau^4 h, h = 1/24 - tau h5, with
-        // h5 = sum_{j>=0} (-tau)^j / (j+5)! (through tau^12) - the Horner chain's value one
-        // step before h
-        float h5 = 1.0f / 479001600.0f;
+        // h5 = sum_{j>=0} (-tau)^j / (j+5)! (through tau^16: below 8e-10 of s4 at tau = 2)
+        // - the Horner chain's value one step before h. The threshold 2 keeps warps whose
+        // groups have tau up to 2 on this branch.
+        float h5 = 1.0f / 20922789888000.0f;       // 1/16!
+        h5 = fmaf(h5, -tau, 1.0f / 1307674368000.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 87178291200.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 6227020800.0f);
+        h5 = fmaf(h5, -tau, 1.0f / 479001600.0f);  // 1/12!
         h5 = fmaf(h5, -tau, 1.0f / 39916800.0f);
         h5 = fmaf(h5, -tau, 1.0f / 3628800.0f);
         h5 = fmaf(h5, -tau, 1.0f / 362880.0f);
@@ -67,10 +72,10 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
         r.d2 = fmaf(1.0f + tau, s4, t2 * fmaf(tau, fmaf(tau, -1.0f / 6.0f, 1.0f / 3.0f), -0.5f));
         // D3 = tau dcub/dtau - 4 cub with dcub/dtau = tau^3 - 6 s4:
         //    = tau^4 - (6 tau + 24) s4 = tau^5 ((6 tau + 24) h5 - 1/4)
-        // (-1/4 against ~1/5: the leading terms cancel by a factor of 5 only)
+        // (-1/4 against ~1/5: the leading terms cancel 5-fold at small tau, 9-fold at 2)
         r.d3 = t4 * tau * fmaf(fmaf(6.0f, tau, 24.0f), h5, -0.25f);
     } else {
-        // no cancellation above tau = 1: one ex2.approx
+        // little cancellation from tau = 2 on: one ex2.approx
         r.p = ex2_approx(tau * -1.44269504088896341f);
         r.e = 1.0f - r.p;
         r.tme = tau - r.e;

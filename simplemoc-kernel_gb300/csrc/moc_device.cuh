@@ -251,12 +251,13 @@ __device__ __forceinline__ float exp_neg_rr(float tau)
 // The exponential terms of the attenuation, accurate for every tau >= 0:
 //   e = 1 - exp(-tau), p = exp(-tau), tme = tau - e,
 //   cub = tau(tau(tau-3)+6) - 6e.
-// For small tau the direct forms cancel (tme ~ tau^2/2, cub ~ tau^4/4). Below tau = 1
+// For small tau the direct forms cancel (tme ~ tau^2/2, cub ~ tau^4/4). Below tau = 2
 // all four come from one Taylor sum, s4 = sum_{k>=4} (-1)^k tau^k / k! (Horner in -tau
-// through tau^12; the first omitted term is below 4e-9 of s4 at tau = 1):
+// through tau^16; the first omitted term is below 8e-10 of s4 at tau = 2):
 //   cub = 6 s4,  tme = tau^2 (1/2 - tau/6) + s4,  e = tau - tme,  p = 1 - e,
-// none of which cancels there (tme <= tau^2/2, e >= 0.63 tau). From tau = 1 on, p comes
-// from the range-reduced exponential and the cubic cancels at most ~30-fold.
+// none of which cancels there (tme <= tau^2/2, e >= 0.43 tau). From tau = 2 on, p comes
+// from the range-reduced exponential and the cubic cancels at most ~5-fold. (The
+// threshold 2 keeps warps whose groups have tau up to 2 on one branch.)
 struct ExpTerms {
     float e, p, tme, cub;
 };
@@ -264,8 +265,12 @@ struct ExpTerms {
 __device__ __forceinline__ ExpTerms exp_terms_stable(float tau)
 {
     ExpTerms r;
-    if (tau < 1.0f) {
-        float h = 1.0f / 479001600.0f;             // 1/12!
+    if (tau < 2.0f) {
+        float h = 1.0f / 20922789888000.0f;        // 1/16!
+        h = fmaf(h, -tau, 1.0f / 1307674368000.0f);  // 1/15!
+        h = fmaf(h, -tau, 1.0f / 87178291200.0f);
+        h = fmaf(h, -tau, 1.0f / 6227020800.0f);
+        h = fmaf(h, -tau, 1.0f / 479001600.0f);    // 1/12!
         h = fmaf(h, -tau, 1.0f / 39916800.0f);     // 1/11!
         h = fmaf(h, -tau, 1.0f / 3628800.0f);
         h = fmaf(h, -tau, 1.0f / 362880.0f);
