@@ -70,3 +70,73 @@ def test_random_configuration(handle, k):
         assert not ff[:, hp.G:].any()
         np.testing.assert_array_equal(psi[:, hp.G:], hp.psi[:, hp.G:])
     print(k, hp.S, hp.T, hp.G, kw, res)
+
+
+def _rel(a, b, floor_frac=1e-3):
+    d = np.abs(a.astype(np.float64) - b)
+    den = np.maximum(np.abs(b), floor_frac * np.sqrt(np.mean(b * b)) + 1e-300)
+    r = d / den
+    return float(r.max()), float(np.sqrt(np.mean(r * r)))
+
+
+@pytest.mark.parametrize("k", range(30))
+def test_random_adjoint(handle, k):
+    """The adjoint on random small problems (group counts, lengths, chunk lengths, groups
+    per lane) against the FP64 CPU adjoint."""
+    import torch
+
+    rng = np.random.default_rng(5000 + k)
+    G = int(rng.choice([1, 3, 16, 33, 64, 70, 128]))
+    w = mocatt.WORKLOADS["adjoint_2M_g64"].with_(
+        regions=int(rng.integers(3, 100)), groups=G, tracks=int(rng.integers(1, 150)),
+        lognormal=(float(rng.uniform(20, 300)), 0.9, 0, int(rng.integers(50, 2000))))
+    hp = mocatt.generate(w)
+    opts = mocatt.default_opts(track_chunk=int(rng.choice([0, -1, 32, 100])),
+                               vec=int(rng.choice([0, 1, 2, 4])))
+    wt = np.zeros((hp.R * hp.I, hp.Gs), np.float32)
+    vt = np.zeros((hp.T, hp.Gs), np.float32)
+    wt[:, :G] = rng.standard_normal((hp.R * hp.I, G))
+    vt[:, :G] = rng.standard_normal((hp.T, G))
+    dp = mocatt.DeviceProblem(hp)
+    ds, dsrc, dpsi = handle.adj(dp, torch.from_numpy(wt).cuda(), torch.from_numpy(vt).cuda(),
+                                opts)
+    assert handle.synchronize() == 0
+    ref = oracle.adj_fp64(hp, wt.astype(np.float64), vt.astype(np.float64))
+    for name, got, r in (("sigT", ds, "d_sigT"), ("source", dsrc, "d_source"),
+                         ("psi_in", dpsi, "d_psi_in")):
+        got = got.cpu().numpy()[:, :G]
+        want = ref[r][:, :G]
+        if not np.any(want):
+            continue
+        mx, rms = _rel(got, want)
+        assert rms <= 1e-4 and mx <= 1e-2, (k, name, mx, rms, G, hp.S, hp.T)
+
+
+@pytest.mark.parametrize("k", range(15))
+def test_random_batch(handle, k):
+    """Random sets of one to four problems (mixed group counts and track lengths) swept by
+    the batching form, each problem against the FP64 oracle."""
+    import ctypes as C
+
+    import torch
+
+    rng = np.random.default_rng(7000 + k)
+    hps = []
+    for p in range(int(rng.integers(1, 5))):
+        G = int(rng.choice([1, 5, 16, 32, 33, 70, 128]))
+        w = mocatt.WORKLOADS["batch_20k_g16"].with_(
+            regions=int(rng.integers(3, 100)), groups=G, tracks=int(rng.integers(1, 400)),
+            seed=100 * k + p,
+            lognormal=(float(rng.uniform(20, 300)), 0.9, 0, int(rng.integers(50, 3000))))
+        hps.append(mocatt.generate(w))
+    dps = [mocatt.DeviceProblem(hp) for hp in hps]
+    arr = (mocatt.MocProblem * len(dps))(*[dp.c_struct() for dp in dps])
+    opts = mocatt.default_opts(track_chunk=int(rng.choice([0, -1, 32])),
+                               vec=int(rng.choice([0, 1, 2])))
+    handle.check(mocatt.lib().moc_attenuate_fwd_batch(
+        handle.ptr, arr, len(dps), C.byref(opts),
+        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    assert handle.synchronize() == 0
+    for hp, dp in zip(hps, dps):
+        parity.check_plain(dp.to_host("psi"), dp.to_host("fine_flux"), oracle.fwd_fp64(hp),
+                           hp.G)
