@@ -34,9 +34,10 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// Every term the reverse sweep needs, accurate for all tau >= 0.
+// Every term the reverse sweep needs, accurate for all tau >= 0 (cub3 = cub / 3,
+// d33 = D3 / 3).
 struct AdjTerms {
-    float e, p, tme, cub, d1, d2, d3;
+    float e, p, tme, cub3, d1, d2, d33;
 };
 
 __device__ __forceinline__ AdjTerms adj_terms(float tau)
@@ -62,7 +63,7 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
         const float h = fmaf(h5, -tau, 1.0f / 24.0f);
         const float t2 = tau * tau, t3 = t2 * tau, t4 = t2 * t2;
         const float s4 = h * t4;
-        r.cub = 6.0f * s4;
+        r.cub3 = 2.0f * s4;
         r.tme = fmaf(t2, fmaf(tau, -1.0f / 6.0f, 0.5f), s4);
         r.e = tau - r.tme;
         r.p = 1.0f - r.e;
@@ -73,17 +74,17 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
         // D3 = tau dcub/dtau - 4 cub with dcub/dtau = tau^3 - 6 s4:
         //    = tau^4 - (6 tau + 24) s4 = tau^5 ((6 tau + 24) h5 - 1/4)
         // (-1/4 against ~1/5: the leading terms cancel 5-fold at small tau, 9-fold at 2)
-        r.d3 = t4 * tau * fmaf(fmaf(6.0f, tau, 24.0f), h5, -0.25f);
+        r.d33 = t4 * tau * fmaf(fmaf(2.0f, tau, 8.0f), h5, -1.0f / 12.0f);
     } else {
         // little cancellation from tau = 2 on: one ex2.approx
         r.p = ex2_approx(tau * -1.44269504088896341f);
         r.e = 1.0f - r.p;
         r.tme = tau - r.e;
-        r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
+        // cub / 3 = tau^2 (tau/3 - 1) + 2 tme; dcub/dtau / 3 = tau (tau - 2) + 2 e
+        r.cub3 = fmaf(tau * tau, fmaf(tau, 1.0f / 3.0f, -1.0f), r.tme + r.tme);
         r.d1 = fmaf(tau, r.e, -2.0f * r.tme);
         r.d2 = fmaf(tau, r.p, -r.e);
-        const float dcub = fmaf(3.0f * tau, tau - 2.0f, 6.0f * r.e);  // 3t^2 - 6t + 6 - 6p
-        r.d3 = fmaf(tau, dcub, -4.0f * r.cub);
+        r.d33 = fmaf(tau, fmaf(tau, tau - 2.0f, r.e + r.e), -4.0f * r.cub3);
     }
     return r;
 }
@@ -211,7 +212,14 @@ __device__ __forceinline__ void red4_if(float4 *p, const float4 &g, int cell, in
 }
 
 // The reverse sweep of one segment for VEC groups: gradient block scattered, lambda
-// carried back (lambda_in = p lambda_out + W e/s).
+// carried back. The forward is built from four functions of (s, tau):
+//   f1 = e/s, f2 = tme/s^2, f3 = reuse, f4 = cub/(3 s^4);
+//   FI = a0 f2 + psi f1 + a1 f3 + a2 f4,   psi' = a0 f1 + a1 f2 + a2 f3 + psi p,
+// and their s-derivatives are f1' = D2/s^2, f2' = D1/s^3, f3' = dreuse/ds,
+// f4' = D3/(3 s^5). So, with lambda = dL/dpsi' and W = weight w[cell]:
+//   dL/da_k  = lambda f_{k+1} + W f_{k+2}                     (k = 0, 1, 2)
+//   dL/ds    = sum_k a_k (lambda f'_{k+1} + W f'_{k+2}) + psi (W f1' - lambda ds p)
+//   lambda  <- lambda p + W f1.
 template <int VEC>
 __device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg<VEC> &sg,
                                                 Vec<VEC> &lam, float4 *gb, int lim)
@@ -224,19 +232,23 @@ __device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg
         const float tau = s * d;
         const AdjTerms x = adj_terms(tau);
         const float rs = rcp_approx(s), rs2 = rs * rs, rs3 = rs2 * rs;
-        const float rs4 = rs2 * rs2, rs5 = rs4 * rs;
-        const float reuse = fmaf(tau, tau - 2.0f, 2.0f * x.e * rs3);
-        const float dreuse = fmaf((2.0f * tau - 2.0f) * tau, rs,
-                                  fmaf(2.0f * tau, x.p, -6.0f * x.e) * rs4);
-        const float fi_s = a0 * x.d1 * rs3 + ps * x.d2 * rs2 + a1 * dreuse +
-                           a2 * x.d3 * rs5 * (1.0f / 3.0f);
-        const float pn_s = a0 * x.d2 * rs2 + a1 * x.d1 * rs3 + a2 * dreuse - ps * x.p * d;
+        const float rs4 = rs2 * rs2;
+        const float f1 = x.e * rs, f2 = x.tme * rs2;
+        const float f3 = fmaf(tau, tau - 2.0f, (x.e + x.e) * rs3);
+        const float f4 = x.cub3 * rs4;
+        const float g1 = x.d2 * rs2, g2 = x.d1 * rs3;
+        const float g3 = fmaf((tau + tau - 2.0f) * tau, rs, fmaf(tau + tau, x.p, -6.0f * x.e) * rs4);
+        const float g4 = x.d33 * rs4 * rs;
         float4 gr;
-        gr.x = fmaf(la, pn_s, W * fi_s);
-        gr.y = fmaf(la, x.e * rs, W * x.tme * rs2);
-        gr.z = fmaf(la, x.tme * rs2, W * reuse);
-        gr.w = fmaf(la, reuse, W * x.cub * rs4 * (1.0f / 3.0f));
-        lam.v[q] = fmaf(la, x.p, W * x.e * rs);
+        gr.y = fmaf(la, f1, W * f2);
+        gr.z = fmaf(la, f2, W * f3);
+        gr.w = fmaf(la, f3, W * f4);
+        float gs = ps * fmaf(W, g1, -la * d * x.p);
+        gs = fmaf(a0, fmaf(la, g1, W * g2), gs);
+        gs = fmaf(a1, fmaf(la, g2, W * g3), gs);
+        gs = fmaf(a2, fmaf(la, g3, W * g4), gs);
+        gr.x = gs;
+        lam.v[q] = fmaf(la, x.p, W * f1);
         red4_if(gb + sg.c * A.fw.Gs + q, gr, sg.c, lim);
     }
 }
