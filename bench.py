@@ -74,7 +74,9 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running; the
+    constructor returns once the first sample is written, so the timed region that
+    follows is covered from its start."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -85,10 +87,21 @@ class ClockSampler:
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        if self.p is not None:
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and self.p.poll() is None:
+                self.f.flush()
+                if os.path.getsize(self.f.name) > 0:
+                    break
+                time.sleep(0.02)
+            # count only what is sampled from here on
+            self.skip = len(open(self.f.name).read().strip().splitlines())
+        else:
+            self.skip = 0
 
     def stop(self) -> dict:
         if self.p is None:
@@ -101,6 +114,7 @@ class ClockSampler:
         self.f.flush()
         self.f.seek(0)
         rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        rows = rows[self.skip:] or rows
         os.unlink(self.f.name)
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
@@ -481,7 +495,7 @@ def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--workload", default="sweep_50M_g128")
