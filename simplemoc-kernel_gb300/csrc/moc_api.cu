@@ -380,7 +380,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (prep && cfg.store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
-                                           o->mu, o->mu2, st, true));
+                                           o->mu, o->mu2, st, true, moc::f32_pairs(cfg.vec)));
     else if (prep)
         MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
                                              p->n_regions, p->n_intervals, p->group_stride,
@@ -595,7 +595,7 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
             sp.map_a = map_a;
             sp.map_b = map_b;
             moc::FwdConfig &mc = X.mcfg[k];
-            mc.vec = moc::auto_vec(p.n_groups);
+            mc.vec = vec;  // the batch's groups per lane: its cell-block layout
             mc.warps_per_block = 8;
             mc.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
             mc.mode = 1;
@@ -674,7 +674,7 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
                                            const_cast<float4 *>(B.prob[k].blk),
                                            probs[k].n_regions, probs[k].n_intervals,
                                            probs[k].group_stride, o->dz, o->zin, o->mu, o->mu2,
-                                           sk, true));
+                                           sk, true, moc::f32_pairs(vec)));
         if (X.on[k]) {
             MOC_CUDA(h, moc::launch_split_records(X.sp[k], X.sw[k], sk));
             MOC_CUDA(h, moc::launch_fwd(X.sp[k], X.mcfg[k], sk));
@@ -702,10 +702,12 @@ moc_status_t prep_blocks(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
     const int store = o->precision == MOC_PREC_BF16   ? moc::STORE_BF16
                       : o->precision == MOC_PREC_FP16 ? moc::STORE_F16
                                                       : moc::STORE_F32;
+    // the layout the sweep's lanes read (pick_config's groups per lane)
+    const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
     if (store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
-                                           o->mu, o->mu2, st, true));
+                                           o->mu, o->mu2, st, true, moc::f32_pairs(vec)));
     else
         MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, store, p->n_regions,
                                              p->n_intervals, p->group_stride, o->dz, o->zin,

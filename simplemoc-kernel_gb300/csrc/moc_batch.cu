@@ -10,6 +10,7 @@
 // that the warps of the persistent kernel consume with one atomicAdd per item. The whole
 // sequence (coefficient passes, queue construction, sweep) is a handful of kernels that
 // the host side captures into a CUDA graph and replays.
+#include "moc_arith.cuh"
 #include "moc_device.cuh"
 #include "moc_internal.h"
 
@@ -139,35 +140,10 @@ __device__ __forceinline__ void attenuate_b(const float4 (&x)[VEC], float ds, fl
                                             const float2 *tab, const BatchParams &B,
                                             Vec<VEC> &psi, Vec<VEC> &tally)
 {
-#pragma unroll
-    for (int k = 0; k < VEC; k++) {
-        const float s = x[k].x, a0 = x[k].y, a1 = x[k].z, a2 = x[k].w;
-        const float ps = psi.v[k];
-        const float tau = __fmul_rn(s, ds);
-        float e, p;
-        if constexpr (EK == EXPK_TABLE) {
-            e = table_lookup(tab, B.tab_n, B.tab_dx, B.tab_max, tau);
-            p = 1.0f - e;
-        } else {
-            p = ex2_approx(tau * -1.44269504088896341f);
-            e = 1.0f - p;
-        }
-        // same arithmetic as the single-problem sweep (attenuate<> in moc_sweep.cu)
-        const float tt = tau * tau;
-        const float tme = tau - e;
-        const float cub3 = fmaf(tt, fmaf(tau, 1.0f / 3.0f, -1.0f), tme + tme);
-        const float rs = rcp_approx(s);
-        const float rs2 = rs * rs;
-        const float e1 = e * rs, t2 = tme * rs2;
-        const float reuse = fmaf(e1 + e1, rs2, fmaf(tau, -2.0f, tt));
-        float fi = fmaf(a0, t2, ps * e1);
-        fi = fmaf(a1, reuse, fi);
-        fi = fmaf(a2 * cub3, rs2 * rs2, fi);
-        tally.v[k] = weight * fi;
-        float pn = fmaf(a1, t2, a0 * e1);
-        pn = fmaf(a2, reuse, pn);
-        psi.v[k] = fmaf(ps, p, pn);
-    }
+    // the same arithmetic as the single-problem sweep, on blocks in the same layout
+    const TableRef tr{tab, B.tab_n, B.tab_dx, B.tab_max};
+    Vec<VEC> pmul;
+    attenuate_row<VEC, EK, f32_pairs(VEC)>(x, ds, weight, tr, psi, tally, pmul);
 }
 
 // 7. the persistent sweep over the queue

@@ -6,7 +6,18 @@
 
 #include "moc_attenuate.h"
 
+// Two groups' FP32 arithmetic per packed .f32x2 instruction where a lane of the sweep holds
+// an even number of groups (bit-identical to the one-group form; -DMOC_PAIRED_FP32=0
+// builds the one-group form everywhere).
+#ifndef MOC_PAIRED_FP32
+#define MOC_PAIRED_FP32 1
+#endif
+
 namespace moc {
+
+constexpr bool PAIRED_FP32 = MOC_PAIRED_FP32 != 0;
+// The sweep with `vec` groups per lane reads FP32 cell blocks in the pair layout (below).
+constexpr bool f32_pairs(int vec) { return PAIRED_FP32 && vec % 2 == 0; }
 
 // The size / enum / alignment checks of moc_attenuate_fwd, and its check that every
 // problem pointer is device (or managed) memory.
@@ -109,9 +120,13 @@ cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStr
 // the first product of kernel.c:250-251 / 311-322 round them.
 // null_row: also write the null cell (1, 0, 0, 0) per group after the last cell (blk
 // then holds R*I + 1 rows).
+// pairs: the pair layout, in which groups 2h and 2h+1 of a cell share two float4,
+// (sigT_2h, sigT_2h+1, q0_2h, q0_2h+1) and (q1mu_2h, q1mu_2h+1, q2mu2_2h, q2mu2_2h+1), so
+// that a lane's loads land every pair of operands of the packed arithmetic in adjacent
+// registers (Gs is a multiple of 4, so pairs never straddle cells).
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st, bool null_row = false);
+                              cudaStream_t st, bool null_row = false, bool pairs = false);
 // The same blocks rounded to bf16 (store = STORE_BF16) or fp16 (STORE_F16), to nearest.
 cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
                                 int R, int I, int Gs, float dz, float zin, float mu,

@@ -158,7 +158,8 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     sp.null_cell = -1;  // no null-cell row in the fixed scratch: the checked segment loop
 
     NA_CUDA(moc::launch_prep_block(p->sigT, p->source, blk, p->n_regions, p->n_intervals,
-                                   p->group_stride, o->dz, o->zin, o->mu, o->mu2, st));
+                                   p->group_stride, o->dz, o->zin, o->mu, o->mu2, st, false,
+                                   moc::f32_pairs(cfg.vec)));
     NA_CUDA(moc::launch_fwd(sp, cfg, st));
     return MOC_OK;
 }

@@ -25,6 +25,7 @@
 //  * segments are branch-free: past the item's end or with a bad index a segment is a
 //    null-cell no-op, idle lanes read group 0, the tally is one predicated reduction.
 // Tallies go out as red.global.add.v4.f32 (one L2 request per lane, 16 bytes).
+#include "moc_arith.cuh"
 #include "moc_device.cuh"
 #include "moc_internal.h"
 
@@ -108,6 +109,26 @@ __global__ void prep_block_kernel(const float *__restrict__ sigT,
     }
 }
 
+// The FP32 blocks in the pair layout: one thread per pair of groups (k, k + 1), k even.
+__global__ void prep_pairs_kernel(const float *__restrict__ sigT,
+                                  const float *__restrict__ source, float4 *__restrict__ blk,
+                                  int R, int I, int Gs, float dz, float zin, float mu,
+                                  float mu2, int null_row)
+{
+    const int64_t n = (int64_t)R * I * Gs;
+    const int64_t n_all = n + (null_row ? Gs : 0);
+    for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; 2 * h < n_all;
+         h += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = 2 * h;
+        const float4 nul = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+        const float4 u = k < n ? cell_block(sigT, source, k, I, Gs, dz, zin, mu, mu2) : nul;
+        const float4 w =
+            k < n ? cell_block(sigT, source, k + 1, I, Gs, dz, zin, mu, mu2) : nul;
+        blk[k] = make_float4(u.x, w.x, u.y, w.y);
+        blk[k + 1] = make_float4(u.z, w.z, u.w, w.w);
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // The per-(segment, group) arithmetic.
 // ------------------------------------------------------------------------------------
@@ -118,7 +139,25 @@ struct Blk {
 
 // Block of VEC groups at element index idx (= cell * Gs + g0). FP32 blocks are 16 bytes
 // per group; BF16/FP16 blocks 8 bytes (four 16-bit values), widened to FP32 on load.
-template <int VEC, int ST>
+// One 16-bit block (four bf16 or fp16 values) widened to FP32.
+template <int ST>
+__device__ __forceinline__ float4 widen(uint2 w)
+{
+    if constexpr (ST == STORE_BF16) {
+        return make_float4(__uint_as_float(w.x << 16), __uint_as_float(w.x & 0xffff0000u),
+                           __uint_as_float(w.y << 16), __uint_as_float(w.y & 0xffff0000u));
+    } else {
+        const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
+        const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
+        return make_float4(lo.x, lo.y, hi.x, hi.y);
+    }
+}
+
+// PAIRS: the lane's groups are consumed two at a time by the packed arithmetic, with each
+// pair's two float4 in the pair layout (sigT_a, sigT_b, q0_a, q0_b), (q1mu_a, q1mu_b,
+// q2mu2_a, q2mu2_b): FP32 blocks are stored that way; 16-bit blocks, stored per group, are
+// widened straight into that order.
+template <int VEC, int ST, bool PAIRS = f32_pairs(VEC)>
 __device__ __forceinline__ void load_blk(const void *base, int idx, Blk<VEC> &b)
 {
     if constexpr (ST == STORE_F32) {
@@ -139,76 +178,30 @@ __device__ __forceinline__ void load_blk(const void *base, int idx, Blk<VEC> &b)
         } else {
             w[0] = __ldg(p);
         }
+        float4 f[VEC];
 #pragma unroll
-        for (int k = 0; k < VEC; k++) {
-            if constexpr (ST == STORE_BF16) {
-                b.v[k] = make_float4(__uint_as_float(w[k].x << 16),
-                                     __uint_as_float(w[k].x & 0xffff0000u),
-                                     __uint_as_float(w[k].y << 16),
-                                     __uint_as_float(w[k].y & 0xffff0000u));
-            } else {
-                const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&w[k].x));
-                const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&w[k].y));
-                b.v[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
+        for (int k = 0; k < VEC; k++) f[k] = widen<ST>(w[k]);
+        if constexpr (PAIRS) {
+#pragma unroll
+            for (int k = 0; k < VEC; k += 2) {
+                b.v[k] = make_float4(f[k].x, f[k + 1].x, f[k].y, f[k + 1].y);
+                b.v[k + 1] = make_float4(f[k].z, f[k + 1].z, f[k].w, f[k + 1].w);
             }
+        } else {
+#pragma unroll
+            for (int k = 0; k < VEC; k++) b.v[k] = f[k];
         }
     }
 }
 
-struct TableRef {
-    const float2 *tab;
-    int n;
-    float dx, max;
-};
-
-// src/cpu/kernel.c:200-332 for VEC groups. Divisions by sigT powers become products with
-// one reciprocal.
+// src/cpu/kernel.c:200-332 for VEC groups (moc_arith.cuh).
 // pmul gets p = exp(-tau) per group (the map mode's product; unused otherwise).
 template <int VEC, int EK>
 __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float weight,
                                           const TableRef &tr, Vec<VEC> &psi,
                                           Vec<VEC> &tally, Vec<VEC> &pmul)
 {
-#pragma unroll
-    for (int k = 0; k < VEC; k++) {
-        const float s = x.v[k].x, a0 = x.v[k].y, a1 = x.v[k].z, a2 = x.v[k].w;
-        const float ps = psi.v[k];
-        const float tau = __fmul_rn(s, ds);  // kept exact: the table index depends on it
-        const float tt = tau * tau;
-        float e, p, tme, cub3;                 // cub3 = (tau(tau(tau-3)+6) - 6e) / 3
-        if constexpr (EK == EXPK_STABLE) {
-            const ExpTerms x = exp_terms_stable(tau);
-            e = x.e;
-            p = x.p;
-            tme = x.tme;
-            cub3 = x.cub * (1.0f / 3.0f);
-        } else {
-            if constexpr (EK == EXPK_TABLE) {
-                e = table_lookup(tr.tab, tr.n, tr.dx, tr.max, tau);
-                p = 1.0f - e;
-            } else {
-                p = ex2_approx(tau * -1.44269504088896341f);
-                e = 1.0f - p;
-            }
-            tme = tau - e;
-            // (tau(tau(tau-3)+6) - 6e)/3 = tau^2 (tau/3 - 1) + 2 (tau - e)
-            cub3 = fmaf(tt, fmaf(tau, 1.0f / 3.0f, -1.0f), tme + tme);
-        }
-        // (q0 tau + (s psi - q0) e)/s^2 == q0 (tau - e)/s^2 + psi e/s exactly, so FI and
-        // psi' share e/s and (tau - e)/s^2; 2e/s^3 = 2 (e/s) / s^2.
-        const float rs = rcp_approx(s);
-        const float rs2 = rs * rs;
-        const float e1 = e * rs, t2 = tme * rs2;
-        const float reuse = fmaf(e1 + e1, rs2, fmaf(tau, -2.0f, tt));
-        float fi = fmaf(a0, t2, ps * e1);
-        fi = fmaf(a1, reuse, fi);
-        fi = fmaf(a2 * cub3, rs2 * rs2, fi);
-        tally.v[k] = weight * fi;
-        float pn = fmaf(a1, t2, a0 * e1);
-        pn = fmaf(a2, reuse, pn);
-        psi.v[k] = fmaf(ps, p, pn);
-        pmul.v[k] = p;
-    }
+    attenuate_row<VEC, EK, f32_pairs(VEC)>(x.v, ds, weight, tr, psi, tally, pmul);
 }
 
 // Lane-parallel descriptor decode of segment j: its cell index and its ds. Out-of-range
@@ -664,12 +657,16 @@ static int grid_for(int64_t n)
 
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st, bool null_row)
+                              cudaStream_t st, bool null_row, bool pairs)
 {
     const int64_t n = (int64_t)R * I * Gs + (null_row ? Gs : 0);
     if (n == 0) return cudaSuccess;
-    prep_block_kernel<STORE_F32><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs, dz,
-                                                               zin, mu, mu2, null_row);
+    if (pairs)  // n is a multiple of Gs, itself a multiple of 4: whole pairs
+        prep_pairs_kernel<<<grid_for(n / 2), 256, 0, st>>>(sigT, source, blk, R, I, Gs, dz,
+                                                            zin, mu, mu2, null_row);
+    else
+        prep_block_kernel<STORE_F32><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
+                                                                   dz, zin, mu, mu2, null_row);
     return cudaGetLastError();
 }
 
