@@ -137,6 +137,7 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
 
 // The forward sweep (persistent, one warp per (track, group chunk) work item).
 constexpr int RING_DEPTH = 8;  // depth of the shared-memory prefetch ring
+constexpr int DESC_RING_F4 = 32;  // the branch-free loop's 64 (cell, ds) pairs per warp
 struct FwdConfig {
     int vec;              // groups per lane: 1, 2, 4
     int warps_per_block;  // 1..16

@@ -300,13 +300,16 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
     }
     if (MODE == MODE_SWEEP && act) psi = ld_psi<VEC>(psi_in + g0, nvalid);
 
-    // Descriptor windows: A = segments [wb, wb+32), B = the next 32.
+    // Descriptor windows: A = segments [wb, wb+32), B = the next 32 (the branch-free loop
+    // keeps them in shared memory instead).
     const int none = RD < 0 ? P.null_cell : -1;
     int64_t wb = beg;
-    int cA, cB;
-    float dA, dB;
-    decode(P, wb + lane, end, none, cA, dA);
-    decode(P, wb + 32 + lane, end, none, cB, dB);
+    int cA = none, cB = none;
+    float dA = 0.0f, dB = 0.0f;
+    if constexpr (RD >= 0) {
+        decode(P, wb + lane, end, none, cA, dA);
+        decode(P, wb + 32 + lane, end, none, cB, dB);
+    }
     auto desc = [&](int64_t j, int &c, float &d) {
         int k = (int)(j - wb);
         if (k >= 32) {
@@ -353,7 +356,9 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
 #pragma unroll
                 for (int k = 0; k < VEC; k++) amul.v[k] *= p.v[k];
             } else {
-                const int idx = c * Gs + g0;
+                // the load's index: it differs from c * Gs + g0 only on lanes past G,
+                // whose reductions lim = 0 turns off
+                const int idx = c * Gs + gl;
                 if constexpr (TL == TALLY_F32) {
                     red_row_if<VEC>(P.ff + idx, tally, c, lim);
                 } else if ((unsigned)c < (unsigned)lim) {
@@ -364,28 +369,41 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
                 }
             }
         };
+        // The warp's 64-entry descriptor ring in shared memory (`ring`, 512 bytes): segment
+        // j's (cell, ds bits) at slot (j - beg) & 63, written lane-parallel a 32-segment
+        // window at a time and read two segments at a time by one broadcast 16-byte load
+        // (one L1 wavefront per pair of segments, where two shuffles per segment took two).
+        int2 *win = reinterpret_cast<int2 *>(ring);
+        auto put = [&](int64_t w0, int slot0) {
+            int c;
+            float d;
+            decode(P, w0 + lane, end, none, c, d);
+            win[slot0 + lane] = make_int2(c, __float_as_int(d));
+        };
+        auto get2 = [&](int slot) {  // slot even: segments slot, slot + 1
+            return reinterpret_cast<const int4 *>(win)[slot >> 1];
+        };
+        put(beg, 0);
+        put(beg + 32, 32);
+        __syncwarp();
         Blk<VEC> b0, b1;
-        int c0 = __shfl_sync(FULL, cA, 0), c1;
-        float d0 = __shfl_sync(FULL, dA, 0), d1;
-        load(c0, b0);
+        int4 q = get2(0);
+        load(q.x, b0);
+        int slot = 0;  // slot of segment wb
         for (; wb < end; wb += 32) {
             const int nk = end - wb < 32 ? (int)(end - wb) : 32;
             for (int k = 0; k < nk; k += 2) {
-                c1 = __shfl_sync(FULL, cA, k + 1);
-                d1 = __shfl_sync(FULL, dA, k + 1);
-                load(c1, b1);
-                step_nb(b0, c0, d0);
-                const int kn = k + 2;
-                const int cs = kn < 32 ? cA : cB;
-                const float ds_ = kn < 32 ? dA : dB;
-                c0 = __shfl_sync(FULL, cs, kn & 31);
-                d0 = __shfl_sync(FULL, ds_, kn & 31);
-                load(c0, b0);
-                step_nb(b1, c1, d1);
+                load(q.z, b1);
+                step_nb(b0, q.x, __int_as_float(q.y));
+                const int4 qn = get2((slot + k + 2) & 63);
+                load(qn.x, b0);
+                step_nb(b1, q.z, __int_as_float(q.w));
+                q = qn;
             }
-            cA = cB;
-            dA = dB;
-            decode(P, wb + 64 + lane, end, none, cB, dB);
+            __syncwarp();  // every lane is past its reads of this window's slots
+            put(wb + 64, slot);
+            __syncwarp();
+            slot ^= 32;
         }
     } else if constexpr (RD == 0) {
         // one segment ahead, in registers (ping-pong, no moves)
@@ -484,7 +502,8 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
 }
 
 // Dynamic shared memory: the exponential table (table mode), then one prefetch ring of
-// RD * VEC * 32 float4 per warp.
+// RD * VEC * 32 float4 per warp (RD > 0) or one 64-segment descriptor ring per warp
+// (RD < 0).
 template <int VEC, int EK, int ST, int TL, int RD, int MODE>
 __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
 {
@@ -497,10 +516,10 @@ __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
         __syncthreads();
         tr = TableRef{s_tab, P.tab_n, P.tab_dx, P.tab_max};
     }
-    float4 *ring = nullptr;
-    if constexpr (RD > 0) {
+    float4 *ring = nullptr;  // the warp's prefetch ring, or its descriptor ring (RD < 0)
+    if constexpr (RD != 0) {
         const int tab_f4 = EK == EXPK_TABLE ? (P.tab_n + 1) / 2 : 0;
-        ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD * VEC * 32);
+        ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD > 0 ? RD * VEC * 32 : DESC_RING_F4);
     }
     const int lane = threadIdx.x & 31;
     int64_t n_items = P.n_items, n_units = P.T;
@@ -700,6 +719,8 @@ size_t fwd_smem_bytes(const FwdConfig &c, int tab_n)
     size_t b = c.exp_kind == EXPK_TABLE ? (size_t)(tab_n + 1) / 2 * sizeof(float4) : 0;
     if (c.prefetch == RING_DEPTH)
         b += (size_t)c.warps_per_block * c.prefetch * c.vec * 32 * sizeof(float4);
+    else if (c.branch_free)
+        b += (size_t)c.warps_per_block * DESC_RING_F4 * sizeof(float4);
     return b;
 }
 
