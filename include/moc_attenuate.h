@@ -45,7 +45,7 @@
 extern "C" {
 #endif
 
-#define MOC_ABI_VERSION 2
+#define MOC_ABI_VERSION 3
 
 typedef enum {
     MOC_OK = 0,
@@ -58,8 +58,10 @@ typedef enum {
     MOC_ERR_BAD_INDEX = 7,       /* checked mode: a segment named a region, interval
                                     or track offset out of range; nothing was added  */
     MOC_ERR_DEVICE_TIMEOUT = 8,  /* a bounded device-side wait gave up               */
-    MOC_ERR_TOO_LARGE = 9        /* the problem exceeds the fixed scratch of
+    MOC_ERR_TOO_LARGE = 9,       /* the problem exceeds the fixed scratch of
                                     moc_attenuate_fwd_noalloc                         */
+    MOC_ERR_BAD_TRACK = 10       /* track generation (moc_tracks.h): a track record is
+                                    invalid or disagrees with the offsets             */
 } moc_status_t;
 
 typedef struct moc_handle_s *moc_handle_t;
@@ -292,7 +294,9 @@ moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *problem,
  * MOC_ERR_BAD_INDEX if any sweep since the last call met a segment whose region or
  * interval was out of range, or a track whose offsets were not inside [0, S]. Such a
  * segment or track is skipped by the sweep (nothing is read or written through its
- * indices); the rest of the sweep completes.
+ * indices); the rest of the sweep completes. MOC_ERR_BAD_TRACK (first) if a
+ * moc_trace_segments call since then met an invalid track record or one whose segment
+ * count disagreed with the offsets (include/moc_tracks.h).
  */
 moc_status_t moc_synchronize(moc_handle_t handle, void *stream);
 

@@ -18,6 +18,7 @@
 
 #include <stdint.h>
 #include "moc_attenuate.h"
+#include "moc_tracks.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -85,6 +86,20 @@ int oracle_adj_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o, const doubl
 double oracle_loss_fp64(const moc_problem_t *p, const moc_fwd_opts_t *o,
                         const double *sigT, const double *source, const double *psi_in,
                         const double *w, const double *v, int32_t group);
+
+/* Track generation (include/moc_tracks.h), oracle/tracks.c. The plan restated from the
+ * header's definition: fills out[0 .. min(n, cap)) and returns n (-1 if invalid). */
+int64_t oracle_tracks_plan(const moc_geometry_t *g, const moc_quadrature_t *q,
+                           moc_track_t *out, int64_t cap);
+/* Segments of every track by sorting all of its crossings: offsets[0 .. n_tracks], and
+ * the descriptors when reg != NULL and they fit in cap. Returns the total (-1 if
+ * invalid). */
+int64_t oracle_trace(const moc_geometry_t *g, const moc_track_t *tracks, int64_t n_tracks,
+                     int64_t *offsets, int32_t *reg, uint8_t *itv, float *ds, int64_t cap);
+/* The same crossings counted with OpenMP over tracks (the timed CPU arm); returns the
+ * total segment count. nthreads <= 0 uses all available threads. */
+int64_t oracle_trace_omp(const moc_geometry_t *g, const moc_track_t *tracks,
+                         int64_t n_tracks, int nthreads);
 
 #ifdef __cplusplus
 }

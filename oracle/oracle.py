@@ -36,6 +36,11 @@ _SIGS = {
     "oracle_fit_fp32": (C.c_int, [_PP, _PO, _P]),
     "oracle_fwd_fp64_coef": (C.c_int, [_PP, _PO, _P, _P, _P, _P, _P, _P, _P, C.c_int]),
     "oracle_loss_fp64": (C.c_double, [_PP, _PO, _P, _P, _P, _P, _P, C.c_int32]),
+    "oracle_tracks_plan": (C.c_int64, [C.POINTER(mocatt.MocGeometry),
+                                       C.POINTER(mocatt.MocQuadrature), _P, C.c_int64]),
+    "oracle_trace": (C.c_int64, [C.POINTER(mocatt.MocGeometry), _P, C.c_int64, _P, _P, _P,
+                                 _P, C.c_int64]),
+    "oracle_trace_omp": (C.c_int64, [C.POINTER(mocatt.MocGeometry), _P, C.c_int64, C.c_int]),
 }
 
 _lib = None
@@ -228,3 +233,42 @@ def pinref_sweep(hp, table_values=None, table_dx=0.0, table_lookup=0.0):
     if rc:
         raise ValueError("pinref rejected the problem")
     return q.psi, q.fine_flux
+
+
+# ---- track generation ------------------------------------------------------------------
+
+def tracks_plan(g, q) -> np.ndarray:
+    """The oracle's restatement of moc_tracks_plan (TRACK_DTYPE array)."""
+    L = lib()
+    n = L.oracle_tracks_plan(C.byref(g), C.byref(q), None, 0)
+    if n < 0:
+        raise ValueError("invalid geometry or quadrature")
+    out = np.zeros(n, mocatt.TRACK_DTYPE)
+    if n:
+        L.oracle_tracks_plan(C.byref(g), C.byref(q), out.ctypes.data, n)
+    return out
+
+
+def trace(g, tracks: np.ndarray):
+    """Segments of every track by sorting all crossings: (offsets, region, interval, ds)."""
+    L = lib()
+    tracks = np.ascontiguousarray(tracks, mocatt.TRACK_DTYPE)
+    T = len(tracks)
+    off = np.zeros(T + 1, np.int64)
+    tp = tracks.ctypes.data if T else None
+    S = L.oracle_trace(C.byref(g), tp, T, off.ctypes.data, None, None, None, 0)
+    if S < 0:
+        raise ValueError("invalid geometry")
+    reg = np.zeros(max(S, 1), np.int32)
+    itv = np.zeros(max(S, 1), np.uint8)
+    ds = np.zeros(max(S, 1), np.float32)
+    L.oracle_trace(C.byref(g), tp, T, off.ctypes.data, reg.ctypes.data, itv.ctypes.data,
+                   ds.ctypes.data, S)
+    return off, reg[:S], itv[:S], ds[:S]
+
+
+def trace_count_omp(g, tracks: np.ndarray, nthreads: int = 0) -> int:
+    """Total segment count, OpenMP over tracks (the timed CPU arm)."""
+    tracks = np.ascontiguousarray(tracks, mocatt.TRACK_DTYPE)
+    return int(lib().oracle_trace_omp(C.byref(g), tracks.ctypes.data if len(tracks) else None,
+                                      len(tracks), nthreads))

@@ -60,6 +60,20 @@ struct moc_handle_s {
     float *table = nullptr;
     int32_t table_n = 0;
     float table_maxval = 0.0f, table_dx = 0.0f, table_lookup = 0.0f;
+    // track generation: scan tile sums, per-track bound offsets, and the scratch that
+    // moc_trace_count walks into (with the arguments of that call, for
+    // moc_trace_segments to recognise it)
+    int64_t *tscan = nullptr, *tbnd = nullptr;
+    size_t tscan_cap = 0, tbnd_cap = 0;
+    int32_t *treg = nullptr;
+    uint8_t *titv = nullptr;
+    float *tds = nullptr;
+    size_t treg_cap = 0, titv_cap = 0, tds_cap = 0;
+    bool tvalid = false;
+    const void *ttracks = nullptr;
+    const int64_t *toff = nullptr;
+    int64_t tT = 0;
+    moc_geometry_t tgeo{};
     int32_t *err = nullptr;              // device error word
     unsigned long long *counter = nullptr;
     int32_t *err_host = nullptr;         // pinned mirror
@@ -909,6 +923,11 @@ moc_status_t moc_destroy(moc_handle_t h)
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
     if (h->blk) cudaFree(h->blk);
+    if (h->tscan) cudaFree(h->tscan);
+    if (h->tbnd) cudaFree(h->tbnd);
+    if (h->treg) cudaFree(h->treg);
+    if (h->titv) cudaFree(h->titv);
+    if (h->tds) cudaFree(h->tds);
     if (h->lo) cudaFree(h->lo);
     if (h->ff64) cudaFree(h->ff64);
     if (h->gblk) cudaFree(h->gblk);
@@ -1351,7 +1370,98 @@ moc_status_t moc_synchronize(moc_handle_t h, void *stream)
     MOC_CUDA(h, cudaStreamSynchronize(st));
     MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));
     MOC_CUDA(h, cudaStreamSynchronize(st));
+    if (*h->err_host & moc::DEVERR_TRACK) return MOC_ERR_BAD_TRACK;
     return *h->err_host ? MOC_ERR_BAD_INDEX : MOC_OK;
+}
+
+// ---- track generation (include/moc_tracks.h; kernels in moc_trace.cu) -----------------
+
+// Reads the error word; a track error is cleared (other bits stay for moc_synchronize).
+moc_status_t take_track_error(moc_handle_t h, cudaStream_t st, bool *bad)
+{
+    MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                st));
+    MOC_CUDA(h, cudaStreamSynchronize(st));
+    *bad = (*h->err_host & moc::DEVERR_TRACK) != 0;
+    if (*bad) {
+        const int32_t rest = *h->err_host & ~moc::DEVERR_TRACK;
+        MOC_CUDA(h, cudaMemcpyAsync(h->err, &rest, sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    st));
+        MOC_CUDA(h, cudaStreamSynchronize(st));
+    }
+    return MOC_OK;
+}
+
+moc_status_t moc_trace_count(moc_handle_t h, const moc_geometry_t *g,
+                             const moc_track_t *d_tracks, int64_t n_tracks,
+                             int64_t *d_track_offsets, int64_t *n_segments, void *stream)
+{
+    if (!h || !moc::trace_geometry_ok(g) || n_tracks < 0 || !d_track_offsets || !n_segments ||
+        (n_tracks > 0 && !d_tracks))
+        return MOC_ERR_INVALID_ARG;
+    if (!aligned(d_tracks, 8) || !aligned(d_track_offsets, 8)) return MOC_ERR_MISALIGNED;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    moc_status_t s;
+    h->tvalid = false;
+    const int64_t T = n_tracks;
+    const size_t scratch = (size_t)moc::trace_scan_scratch(T) * sizeof(int64_t);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->tscan), &h->tscan_cap, scratch))) return s;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->tbnd), &h->tbnd_cap,
+                    (size_t)(T + 1) * sizeof(int64_t))))
+        return s;
+    // the scratch layout: one slot per track, sized by an upper bound of its count
+    MOC_CUDA(h, moc::launch_trace_bound(g, d_tracks, T, h->tbnd, h->tscan, h->err, st));
+    int64_t B = 0;
+    MOC_CUDA(h, cudaMemcpyAsync(&B, h->tbnd + T, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    MOC_CUDA(h, cudaStreamSynchronize(st));
+    const size_t nb = (size_t)(B > 0 ? B : 1);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->treg), &h->treg_cap, nb * 4)) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->titv), &h->titv_cap, nb)) ||
+        (s = ensure(h, reinterpret_cast<void **>(&h->tds), &h->tds_cap, nb * 4)))
+        return s;
+    // one walk per track into the scratch, the counts scanned into the offsets
+    MOC_CUDA(h, moc::launch_trace_walk(g, d_tracks, T, h->tbnd, d_track_offsets, h->tscan,
+                                       h->treg, h->titv, h->tds, h->err, st));
+    int64_t total = 0;
+    MOC_CUDA(h, cudaMemcpyAsync(&total, d_track_offsets + T, sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, st));
+    bool bad = false;
+    if ((s = take_track_error(h, st, &bad))) return s;
+    *n_segments = total;
+    if (bad) return MOC_ERR_BAD_TRACK;
+    h->tvalid = true;
+    h->ttracks = d_tracks;
+    h->toff = d_track_offsets;
+    h->tT = T;
+    h->tgeo = *g;
+    return MOC_OK;
+}
+
+moc_status_t moc_trace_segments(moc_handle_t h, const moc_geometry_t *g,
+                                const moc_track_t *d_tracks, int64_t n_tracks,
+                                const int64_t *d_track_offsets, int32_t *d_seg_region,
+                                uint8_t *d_seg_interval, float *d_seg_ds, void *stream)
+{
+    if (!h || !moc::trace_geometry_ok(g) || n_tracks < 0 || !d_track_offsets ||
+        (n_tracks > 0 && (!d_tracks || !d_seg_region || !d_seg_interval || !d_seg_ds)))
+        return MOC_ERR_INVALID_ARG;
+    if (!aligned(d_tracks, 8) || !aligned(d_track_offsets, 8) || !aligned(d_seg_region, 4) ||
+        !aligned(d_seg_ds, 4))
+        return MOC_ERR_MISALIGNED;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // after moc_trace_count on the same arguments: copy its walk out of the scratch
+    if (h->tvalid && h->ttracks == d_tracks && h->toff == d_track_offsets &&
+        h->tT == n_tracks && std::memcmp(&h->tgeo, g, sizeof(*g)) == 0) {
+        MOC_CUDA(h, moc::launch_trace_compact(d_tracks, n_tracks, h->tbnd, d_track_offsets,
+                                              h->treg, h->titv, h->tds, d_seg_region,
+                                              d_seg_interval, d_seg_ds, st));
+        return MOC_OK;
+    }
+    MOC_CUDA(h, moc::launch_trace_emit(g, d_tracks, n_tracks, d_track_offsets, d_seg_region,
+                                       d_seg_interval, d_seg_ds, h->err, st));
+    return MOC_OK;
 }
 
 moc_status_t moc_build_exp_table(int32_t n_points, float max_val, float *values, float *dx,
@@ -1411,6 +1521,7 @@ const char *moc_status_string(moc_status_t s)
     case MOC_ERR_BAD_INDEX: return "segment index or track offset out of range";
     case MOC_ERR_DEVICE_TIMEOUT: return "device wait timed out";
     case MOC_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
+    case MOC_ERR_BAD_TRACK: return "track record invalid or inconsistent with the offsets";
     }
     return "unknown status";
 }

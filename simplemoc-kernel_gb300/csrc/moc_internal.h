@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "moc_attenuate.h"
+#include "moc_tracks.h"
 
 // Two groups' FP32 arithmetic per packed .f32x2 instruction where a lane of the sweep holds
 // an even number of groups (bit-identical to the one-group form; -DMOC_PAIRED_FP32=0
@@ -28,6 +29,7 @@ bool all_device_accessible(const moc_problem_t *p);
 enum : int32_t {
     DEVERR_OFFSETS = 1,  // a track's [begin, end) is not inside [0, S]
     DEVERR_INDEX = 2,    // a segment's region or interval is out of range
+    DEVERR_TRACK = 4,    // track generation: a track record is invalid
 };
 
 // How 1 - exp(-tau) and the cancelling terms are evaluated.
@@ -248,5 +250,25 @@ int adj_map_blocks_per_sm(int vec);
 cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,
                               int G, int Gs, const float *jac27, float mu, float mu2,
                               cudaStream_t st);
+
+// Track generation (moc_trace.cu). Scratch of a scan over T entries:
+// trace_scan_scratch(T) int64. Bound: per-track upper bounds of the segment counts,
+// scanned into bnd[0 .. T] (the scratch layout). Walk: every track once into its scratch
+// slot, counts scanned into off[0 .. T]. Compact: scratch to the caller's arrays. Emit: a
+// second walk straight into the caller's arrays at off. Bad records set DEVERR_TRACK.
+bool trace_geometry_ok(const moc_geometry_t *g);
+int64_t trace_scan_scratch(int64_t n_tracks);
+cudaError_t launch_trace_bound(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
+                               int64_t *bnd, int64_t *scratch, int32_t *err, cudaStream_t st);
+cudaError_t launch_trace_walk(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
+                              const int64_t *bnd, int64_t *off, int64_t *scratch, int32_t *sreg,
+                              uint8_t *sitv, float *sds, int32_t *err, cudaStream_t st);
+cudaError_t launch_trace_compact(const moc_track_t *tr, int64_t T, const int64_t *bnd,
+                                 const int64_t *off, const int32_t *sreg, const uint8_t *sitv,
+                                 const float *sds, int32_t *reg, uint8_t *itv, float *ds,
+                                 cudaStream_t st);
+cudaError_t launch_trace_emit(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
+                              const int64_t *off, int32_t *reg, uint8_t *itv, float *ds,
+                              int32_t *err, cudaStream_t st);
 
 }  // namespace moc

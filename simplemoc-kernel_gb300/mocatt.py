@@ -34,6 +34,7 @@ MOC_ERR_OUT_OF_MEMORY = 6
 MOC_ERR_BAD_INDEX = 7
 MOC_ERR_DEVICE_TIMEOUT = 8
 MOC_ERR_TOO_LARGE = 9
+MOC_ERR_BAD_TRACK = 10
 
 MOC_EXP_FULL = 0
 MOC_EXP_TABLE = 1
@@ -81,6 +82,27 @@ class MocTuneResult(C.Structure):
                 ("candidate_warps", C.c_int32 * 16), ("candidate_ms", C.c_float * 16)]
 
 
+class MocGeometry(C.Structure):
+    """moc_geometry_t (include/moc_tracks.h)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("n_rings", C.c_int32),
+                ("n_axial", C.c_int32), ("n_intervals", C.c_int32), ("reserved", C.c_int32),
+                ("pitch", C.c_double), ("fuel_radius", C.c_double), ("height", C.c_double)]
+
+
+class MocQuadrature(C.Structure):
+    """moc_quadrature_t (include/moc_tracks.h)."""
+    _fields_ = [("n_azim", C.c_int32), ("n_polar", C.c_int32),
+                ("both_directions", C.c_int32), ("reserved", C.c_int32),
+                ("spacing", C.c_double), ("axial_spacing", C.c_double)]
+
+
+# moc_track_t as a numpy record (112 bytes)
+TRACK_DTYPE = np.dtype([(n, np.float64) for n in (
+    "x0", "y0", "ux", "uy", "rux", "ruy", "ta", "tb", "za", "cot", "rcot", "rsin")] +
+    [(n, np.int32) for n in ("azim", "polar", "reversed", "reserved")])
+assert TRACK_DTYPE.itemsize == 112
+
+
 class SynthSpec(C.Structure):
     _fields_ = [
         ("seed", C.c_uint64), ("n_regions", C.c_int32), ("n_intervals", C.c_int32),
@@ -114,6 +136,15 @@ ABI = {
     "moc_status_string": (C.c_char_p, [C.c_int]),
     "moc_last_error": (C.c_char_p, [_P]),
     "moc_abi_version": (C.c_int32, []),
+    "moc_geometry_regions": (C.c_int32, [C.POINTER(MocGeometry)]),
+    "moc_geometry_volumes": (C.c_int, [C.POINTER(MocGeometry), _P]),
+    "moc_tracks_plan": (C.c_int, [C.POINTER(MocGeometry), C.POINTER(MocQuadrature), _P,
+                                  C.c_int64, C.POINTER(C.c_int64)]),
+    "moc_tracks_weight": (C.c_double, [C.POINTER(MocQuadrature)]),
+    "moc_trace_count": (C.c_int, [_P, C.POINTER(MocGeometry), _P, C.c_int64, _P,
+                                  C.POINTER(C.c_int64), _P]),
+    "moc_trace_segments": (C.c_int, [_P, C.POINTER(MocGeometry), _P, C.c_int64, _P, _P,
+                                     _P, _P, _P]),
 }
 SYNTH_ABI = {
     "moc_synth_spec_init": (None, [C.POINTER(SynthSpec), C.c_uint64, C.c_int32, C.c_int32,
@@ -364,6 +395,51 @@ def synth_randint(seed: int, tag: int, n: int, bound: int) -> np.ndarray:
 # ------------------------------------------------------------------------------------
 # Device side (torch is only the allocator and stream provider here)
 # ------------------------------------------------------------------------------------
+# ---- track generation (include/moc_tracks.h) -------------------------------------------
+
+def geometry(nx=17, ny=17, n_rings=3, n_axial=40, n_intervals=5, pitch=1.26,
+             fuel_radius=0.54, height=200.0) -> MocGeometry:
+    """A pin lattice (defaults: a 17 x 17 assembly, 1.26 cm pitch, 200 cm tall)."""
+    return MocGeometry(nx, ny, n_rings, n_axial, n_intervals, 0, pitch, fuel_radius, height)
+
+
+def quadrature(n_azim=8, n_polar=4, spacing=0.1, axial_spacing=1.0,
+               both_directions=0) -> MocQuadrature:
+    return MocQuadrature(n_azim, n_polar, both_directions, 0, spacing, axial_spacing)
+
+
+def geometry_regions(g: MocGeometry) -> int:
+    return int(lib().moc_geometry_regions(C.byref(g)))
+
+
+def geometry_volumes(g: MocGeometry) -> np.ndarray:
+    """Volume of every (region, interval) cell, [n_regions * n_intervals] float64."""
+    v = np.empty(geometry_regions(g) * g.n_intervals, np.float64)
+    st = lib().moc_geometry_volumes(C.byref(g), v.ctypes.data)
+    if st:
+        raise MocError(st)
+    return v
+
+
+def tracks_plan(g: MocGeometry, q: MocQuadrature) -> np.ndarray:
+    """moc_tracks_plan: the tracks as a TRACK_DTYPE array (host)."""
+    n = C.c_int64()
+    L = lib()
+    st = L.moc_tracks_plan(C.byref(g), C.byref(q), None, 0, C.byref(n))
+    if st:
+        raise MocError(st)
+    out = np.zeros(n.value, TRACK_DTYPE)
+    st = L.moc_tracks_plan(C.byref(g), C.byref(q), out.ctypes.data if n.value else None,
+                           n.value, C.byref(n))
+    if st:
+        raise MocError(st)
+    return out
+
+
+def tracks_weight(q: MocQuadrature) -> float:
+    return float(lib().moc_tracks_weight(C.byref(q)))
+
+
 class DeviceProblem:
     """A problem resident on the GPU (torch tensors), and its C struct."""
 
@@ -431,6 +507,28 @@ class Handle:
                                            d_src.data_ptr(), d_psi.data_ptr(),
                                            C.c_void_p(s.cuda_stream)))
         return d_sig, d_src, d_psi
+
+    def trace(self, g: MocGeometry, d_tracks, n_tracks: int, stream=None):
+        """moc_trace_count + moc_trace_segments: the CSR descriptors of the tracks
+        (d_tracks: a device tensor holding n_tracks moc_track_t records). Returns device
+        tensors (track_offsets int64 [T+1], seg_region int32, seg_interval uint8,
+        seg_ds float32)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        dev = d_tracks.device
+        off = torch.empty(n_tracks + 1, dtype=torch.int64, device=dev)
+        S = C.c_int64()
+        L = lib()
+        self.check(L.moc_trace_count(self._h, C.byref(g), d_tracks.data_ptr(), n_tracks,
+                                     off.data_ptr(), C.byref(S), C.c_void_p(s.cuda_stream)))
+        n = S.value
+        reg = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        itv = torch.empty(max(n, 1), dtype=torch.uint8, device=dev)
+        ds = torch.empty(max(n, 1), dtype=torch.float32, device=dev)
+        self.check(L.moc_trace_segments(self._h, C.byref(g), d_tracks.data_ptr(), n_tracks,
+                                        off.data_ptr(), reg.data_ptr(), itv.data_ptr(),
+                                        ds.data_ptr(), C.c_void_p(s.cuda_stream)))
+        return off, reg[:n], itv[:n], ds[:n]
 
     def fwd_host(self, hp: HostProblem, opts: MocFwdOpts | None = None):
         opts = opts or default_opts()

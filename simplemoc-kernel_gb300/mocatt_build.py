@@ -30,7 +30,10 @@ NVCC_FLAGS = ARCH + [
     "-I" + INCLUDE, "-I" + CSRC,
 ]
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu", "moc_adjoint.cu",
-              "moc_batch.cu", "moc_split.cu"]
+              "moc_batch.cu", "moc_split.cu", "moc_trace.cu"]
+# Per-file flags: the track walk rounds every FP64 operation on its own, as the C oracle
+# compiled with -ffp-contract=off does, so its descriptors match the oracle's bit for bit.
+EXTRA_FLAGS = {"moc_trace.cu": ["-fmad=false"]}
 
 LIB = os.path.join(BUILD, "libmocatt.so")
 SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")
@@ -81,7 +84,7 @@ def build(verbose: bool = False) -> dict:
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if _stale(o, [s] + hdrs):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc()] + NVCC_FLAGS + EXTRA_FLAGS.get(src, []) + ["-c", s, "-o", o])
     synth_src = os.path.join(HOST, "synth.c")
     synth_cmd = None
     if _stale(SYNTH_LIB, [synth_src, os.path.join(INCLUDE, "moc_synth.h")]):

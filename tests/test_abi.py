@@ -27,7 +27,7 @@ def exported(lib_path):
 
 def test_every_declared_symbol_is_exported():
     syms = exported(os.path.join(mocatt.BUILD, "libmocatt.so"))
-    decl = declared_functions("moc_attenuate.h")
+    decl = declared_functions("moc_attenuate.h") + declared_functions("moc_tracks.h")
     assert decl, "no declarations found"
     missing = [n for n in decl if n not in syms]
     assert not missing, missing
@@ -40,7 +40,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_library_loads_and_reports_version():
     L = mocatt.lib()
-    assert L.moc_abi_version() == 2
+    assert L.moc_abi_version() == 3
     assert L.moc_status_string(mocatt.MOC_ERR_BAD_INDEX).decode().startswith("segment")
     assert L.moc_status_string(999) == b"unknown status"
 
