@@ -169,14 +169,14 @@ def load_peaks() -> dict:
 def run_peaks() -> dict:
     lib = C.CDLL(os.path.join(PKG, "_build", "libmocpeaks.so"))
     lib.mocpeak_run.restype = C.c_int
-    res = (C.c_double * 9)()
-    rc = lib.mocpeak_run(res, 9)
+    res = (C.c_double * 10)()
+    rc = lib.mocpeak_run(res, 10)
     if rc:
         raise RuntimeError(f"mocpeak_run failed: {rc}")
     out = {"l2_stream_read_gbs": res[0], "l2_row_gather_hashed_gbs": res[1],
            "l2_row_reduce_hashed_gbs": res[2], "fp32_fma_tflops": res[3],
            "mufu_ex2_gops": res[4], "hbm_read_gbs": res[5], "l2_row_gather_gbs": res[6],
-           "l2_row_reduce_gbs": res[7], "l2_mix_gbs": res[8],
+           "l2_row_reduce_gbs": res[7], "l2_mix_gbs": res[8], "fp64_fma_tflops": res[9],
            "mix": "four random 512-byte row gathers per 512-byte red.v4 row reduction "
                   "(the sweep's 16 B gathered : 4 B reduced per segment*group)",
            "how": "simplemoc-kernel_gb300/csrc/moc_peaks.cu via bench.py --peaks: "

@@ -65,6 +65,8 @@ struct moc_handle_s {
     // moc_trace_segments to recognise it)
     int64_t *tscan = nullptr, *tbnd = nullptr;
     size_t tscan_cap = 0, tbnd_cap = 0;
+    double *ttab = nullptr;              // the walk's tables of the geometry
+    size_t ttab_cap = 0;
     int32_t *treg = nullptr;
     uint8_t *titv = nullptr;
     float *tds = nullptr;
@@ -925,6 +927,7 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->blk) cudaFree(h->blk);
     if (h->tscan) cudaFree(h->tscan);
     if (h->tbnd) cudaFree(h->tbnd);
+    if (h->ttab) cudaFree(h->ttab);
     if (h->treg) cudaFree(h->treg);
     if (h->titv) cudaFree(h->titv);
     if (h->tds) cudaFree(h->tds);
@@ -1376,6 +1379,17 @@ moc_status_t moc_synchronize(moc_handle_t h, void *stream)
 
 // ---- track generation (include/moc_tracks.h; kernels in moc_trace.cu) -----------------
 
+// The walk's tables of geometry g in h->ttab.
+moc_status_t trace_tables(moc_handle_t h, const moc_geometry_t *g, cudaStream_t st)
+{
+    moc_status_t s;
+    const size_t n = (size_t)moc::trace_table_len(g);
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->ttab), &h->ttab_cap, n * sizeof(double))))
+        return s;
+    MOC_CUDA(h, moc::launch_trace_tables(g, h->ttab, st));
+    return MOC_OK;
+}
+
 // Reads the error word; a track error is cleared (other bits stay for moc_synchronize).
 moc_status_t take_track_error(moc_handle_t h, cudaStream_t st, bool *bad)
 {
@@ -1420,9 +1434,10 @@ moc_status_t moc_trace_count(moc_handle_t h, const moc_geometry_t *g,
         (s = ensure(h, reinterpret_cast<void **>(&h->titv), &h->titv_cap, nb)) ||
         (s = ensure(h, reinterpret_cast<void **>(&h->tds), &h->tds_cap, nb * 4)))
         return s;
+    if ((s = trace_tables(h, g, st))) return s;
     // one walk per track into the scratch, the counts scanned into the offsets
-    MOC_CUDA(h, moc::launch_trace_walk(g, d_tracks, T, h->tbnd, d_track_offsets, h->tscan,
-                                       h->treg, h->titv, h->tds, h->err, st));
+    MOC_CUDA(h, moc::launch_trace_walk(g, h->ttab, d_tracks, T, h->tbnd, d_track_offsets,
+                                       h->tscan, h->treg, h->titv, h->tds, h->err, st));
     int64_t total = 0;
     MOC_CUDA(h, cudaMemcpyAsync(&total, d_track_offsets + T, sizeof(int64_t),
                                 cudaMemcpyDeviceToHost, st));
@@ -1459,8 +1474,10 @@ moc_status_t moc_trace_segments(moc_handle_t h, const moc_geometry_t *g,
                                               d_seg_interval, d_seg_ds, st));
         return MOC_OK;
     }
-    MOC_CUDA(h, moc::launch_trace_emit(g, d_tracks, n_tracks, d_track_offsets, d_seg_region,
-                                       d_seg_interval, d_seg_ds, h->err, st));
+    moc_status_t s;
+    if ((s = trace_tables(h, g, st))) return s;
+    MOC_CUDA(h, moc::launch_trace_emit(g, h->ttab, d_tracks, n_tracks, d_track_offsets,
+                                       d_seg_region, d_seg_interval, d_seg_ds, h->err, st));
     return MOC_OK;
 }
 

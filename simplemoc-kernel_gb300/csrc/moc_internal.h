@@ -260,15 +260,19 @@ bool trace_geometry_ok(const moc_geometry_t *g);
 int64_t trace_scan_scratch(int64_t n_tracks);
 cudaError_t launch_trace_bound(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
                                int64_t *bnd, int64_t *scratch, int32_t *err, cudaStream_t st);
-cudaError_t launch_trace_walk(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
-                              const int64_t *bnd, int64_t *off, int64_t *scratch, int32_t *sreg,
-                              uint8_t *sitv, float *sds, int32_t *err, cudaStream_t st);
+// Tables of the walk (grid lines, pin centres, fine planes): trace_table_len(g) doubles.
+int64_t trace_table_len(const moc_geometry_t *g);
+cudaError_t launch_trace_tables(const moc_geometry_t *g, double *tab, cudaStream_t st);
+cudaError_t launch_trace_walk(const moc_geometry_t *g, const double *tab, const moc_track_t *tr,
+                              int64_t T, const int64_t *bnd, int64_t *off, int64_t *scratch,
+                              int32_t *sreg, uint8_t *sitv, float *sds, int32_t *err,
+                              cudaStream_t st);
 cudaError_t launch_trace_compact(const moc_track_t *tr, int64_t T, const int64_t *bnd,
                                  const int64_t *off, const int32_t *sreg, const uint8_t *sitv,
                                  const float *sds, int32_t *reg, uint8_t *itv, float *ds,
                                  cudaStream_t st);
-cudaError_t launch_trace_emit(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
-                              const int64_t *off, int32_t *reg, uint8_t *itv, float *ds,
-                              int32_t *err, cudaStream_t st);
+cudaError_t launch_trace_emit(const moc_geometry_t *g, const double *tab, const moc_track_t *tr,
+                              int64_t T, const int64_t *off, int32_t *reg, uint8_t *itv,
+                              float *ds, int32_t *err, cudaStream_t st);
 
 }  // namespace moc

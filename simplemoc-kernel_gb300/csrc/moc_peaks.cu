@@ -122,6 +122,18 @@ __global__ void fma_chains(float *out, int iters, float a, float b)
     if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+__global__ void dfma_chains(double *out, int iters, double a, double b)
+{
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1234.5) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 __global__ void ex2_chains(float *out, int iters)
 {
     float x0 = threadIdx.x * 1e-3f, x1 = x0 + 0.1f, x2 = x0 + 0.2f, x3 = x0 + 0.3f;
@@ -198,6 +210,16 @@ extern "C" int mocpeak_run(double *res, int n_res)
 
     ms = time_ms([&] { stream_read<<<blocks, threads>>>((const float4 *)hbm, hbm_bytes / 16, 1, out, 1); }, 5);
     res[5] = (double)hbm_bytes / (ms * 1e-3) / 1e9;
+
+    if (n_res >= 10) {
+        double *dout = nullptr;
+        if (cudaMalloc(&dout, (size_t)blocks * threads * sizeof(double)) == cudaSuccess) {
+            const int diters = 2000;
+            ms = time_ms([&] { dfma_chains<<<blocks, threads>>>(dout, diters, 0.999, 1e-3); }, 5);
+            res[9] = (double)blocks * threads * diters * 8 * 2.0 / (ms * 1e-3) / 1e12;
+            cudaFree(dout);
+        }
+    }
 
     if (n_res >= 9) {
         // 2^17 rows of 512 B (64 MiB) to gather from, 2^15 tally rows (16 MiB) to reduce into

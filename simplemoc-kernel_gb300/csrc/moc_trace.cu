@@ -51,7 +51,30 @@ struct TraceGeo {
     int nx, ny, K, n_axial, n_int, NZ;
     double P, rP, dz, rdz;
     double r2[MOC_TRACKS_MAX_RINGS];  // ring radii squared, equal areas
+    // device tables (trace_tables): grid lines i P (i = 0..nx, j = 0..ny), pin centres
+    // (i + 1/2) P, fine planes m dz (m = 0..NZ); each entry the same rounded product the
+    // oracle forms, so the walk needs no int-to-double conversion per crossing
+    const double *lx, *ly, *cx, *cy, *pz;
 };
+
+// Entries of the tables of a geometry: (nx + 1) + (ny + 1) + nx + ny + (NZ + 1).
+int64_t table_len(const moc_geometry_t *g)
+{
+    return 2 * ((int64_t)g->nx + g->ny) + 3 + (int64_t)g->n_axial * g->n_intervals;
+}
+
+// floor(x) clamped to [0, n - 1], from the bits of x (exact; integer pipe). Negative x
+// (and -0) give 0, as floor's -1 (or 0) clamped does.
+__host__ __device__ __forceinline__ int floor_clamp(double x, int n)
+{
+    const int64_t b = key(x);
+    if (b < 0) return 0;
+    const int e = (int)(b >> 52) - 1023;
+    if (e < 0) return 0;
+    if (e >= 31) return n - 1;
+    const int64_t v = ((b & ((1ll << 52) - 1)) | (1ll << 52)) >> (52 - e);
+    return v >= n ? n - 1 : (int)v;
+}
 
 bool geo_ok(const moc_geometry_t *g)
 {
@@ -90,21 +113,52 @@ TraceGeo trace_geo(const moc_geometry_t *g)
     return G;
 }
 
+TraceGeo trace_geo(const moc_geometry_t *g, const double *tab)
+{
+    TraceGeo G = trace_geo(g);
+    G.lx = tab;
+    G.ly = G.lx + (G.nx + 1);
+    G.cx = G.ly + (G.ny + 1);
+    G.cy = G.cx + G.nx;
+    G.pz = G.cy + G.ny;
+    return G;
+}
+
+__global__ void trace_tables_kernel(const TraceGeo G, double *tab)
+{
+    const int n = 2 * (G.nx + G.ny) + 3 + G.NZ;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int j = i;
+        double v;
+        if (j <= G.nx) {
+            v = (double)j * G.P;
+        } else if ((j -= G.nx + 1) <= G.ny) {
+            v = (double)j * G.P;
+        } else if ((j -= G.ny + 1) < G.nx) {
+            v = ((double)j + 0.5) * G.P;
+        } else if ((j -= G.nx) < G.ny) {
+            v = ((double)j + 0.5) * G.P;
+        } else {
+            j -= G.ny;
+            v = (double)j * G.dz;
+        }
+        tab[i] = v;
+    }
+}
+
 // Region and interval of the point at t (the midpoint of a segment).
 __host__ __device__ __forceinline__ void classify(const TraceGeo &G, const moc_track_t &tr,
                                                   double tm, int32_t &region, int &itv)
 {
     const double xm = tr.x0 + tm * tr.ux, ym = tr.y0 + tm * tr.uy;
     const double zm = tr.za + (tm - tr.ta) * tr.cot;
-    int ix = (int)floor(xm * G.rP), iy = (int)floor(ym * G.rP);
-    ix = ix < 0 ? 0 : (ix >= G.nx ? G.nx - 1 : ix);
-    iy = iy < 0 ? 0 : (iy >= G.ny ? G.ny - 1 : iy);
-    const double ddx = xm - ((double)ix + 0.5) * G.P, ddy = ym - ((double)iy + 0.5) * G.P;
-    const double rr = ddx * ddx + ddy * ddy;
+    const int ix = floor_clamp(xm * G.rP, G.nx), iy = floor_clamp(ym * G.rP, G.ny);
+    const double ddx = xm - G.cx[ix], ddy = ym - G.cy[iy];
+    const double rr = ddx * ddx + ddy * ddy;  // >= +0: ordered by its key
+    const int64_t kr = key(rr);
     int k = 0;
-    while (k < G.K && !(rr < G.r2[k])) k++;
-    int f = (int)floor(zm * G.rdz);
-    f = f < 0 ? 0 : (f >= G.NZ ? G.NZ - 1 : f);
+    while (k < G.K && !(kr < key(G.r2[k]))) k++;
+    const int f = floor_clamp(zm * G.rdz, G.NZ);
     const int a = f / G.n_int;
     itv = f - a * G.n_int;
     region = ((iy * G.nx + ix) * (G.K + 1) + k) * G.n_axial + a;
@@ -142,12 +196,8 @@ __host__ __device__ int64_t walk(const TraceGeo &G, const moc_track_t &tr, int64
     if (sx < 0 && ix > G.nx) ix = G.nx;
     if (sy > 0 && iy < -1) iy = -1;
     if (sy < 0 && iy > G.ny) iy = G.ny;
-    auto line_x = [&](int i) {
-        return (i < 0 || i > G.nx) ? INF : ((double)i * G.P - tr.x0) * tr.rux;
-    };
-    auto line_y = [&](int j) {
-        return (j < 0 || j > G.ny) ? INF : ((double)j * G.P - tr.y0) * tr.ruy;
-    };
+    auto line_x = [&](int i) { return (i < 0 || i > G.nx) ? INF : (G.lx[i] - tr.x0) * tr.rux; };
+    auto line_y = [&](int j) { return (j < 0 || j > G.ny) ? INF : (G.ly[j] - tr.y0) * tr.ruy; };
     int ixn = sx > 0 ? ix + 1 : ix, iyn = sy > 0 ? iy + 1 : iy;
     double txn = sx ? line_x(ixn) : INF, tyn = sy ? line_y(iyn) : INF;
     // ring crossings of the current cell: entering k = K-1 .. kmin, leaving kmin .. K-1
@@ -157,18 +207,28 @@ __host__ __device__ int64_t walk(const TraceGeo &G, const moc_track_t &tr, int64
         kmin = G.K;
         e = 0;
         if (ix < 0 || ix >= G.nx || iy < 0 || iy >= G.ny) return;
-        const double dxc = ((double)ix + 0.5) * G.P - tr.x0;
-        const double dyc = ((double)iy + 0.5) * G.P - tr.y0;
+        const double dxc = G.cx[ix] - tr.x0;
+        const double dyc = G.cy[iy] - tr.y0;
         w = dxc * tr.ux + dyc * tr.uy;
         const double dp = dxc * tr.uy - dyc * tr.ux;
         dp2 = dp * dp;
-        while (kmin > 0 && G.r2[kmin - 1] - dp2 > 0.0) kmin--;
+        // r2 - dp2 > 0 exactly when r2 > dp2 (both >= 0: ordered by their keys)
+        const int64_t kd = key(dp2);
+        while (kmin > 0 && kd < key(G.r2[kmin - 1])) kmin--;
     };
+    // a ring's leaving crossing reuses the half-chord its entering one computed (every
+    // entering event of the cell is evaluated, in order, before any leaving one)
+    double hk[MOC_TRACKS_MAX_RINGS];
     auto ring_event = [&]() {
         const int nk = G.K - kmin;
         if (e >= 2 * nk) return INF;
-        if (e < nk) return w - sqrt(G.r2[G.K - 1 - e] - dp2);
-        return w + sqrt(G.r2[kmin + e - nk] - dp2);
+        if (e < nk) {
+            const int kk = G.K - 1 - e;
+            const double h = sqrt(G.r2[kk] - dp2);
+            hk[kk] = h;
+            return w - h;
+        }
+        return w + hk[kmin + e - nk];
     };
     setup_cell();
     double tcn = ring_event();
@@ -176,7 +236,7 @@ __host__ __device__ int64_t walk(const TraceGeo &G, const moc_track_t &tr, int64
     int m = (int)fmax(fmin(floor(tr.za * G.rdz), (double)G.NZ + 1.0), -1.0);
     m = dm > 0 ? (m - 1 < 0 ? 0 : m - 1) : (m + 2 > G.NZ ? G.NZ : m + 2);
     auto plane = [&](int mm) {
-        return (mm < 0 || mm > G.NZ) ? INF : tr.ta + ((double)mm * G.dz - tr.za) * tr.rcot;
+        return (mm < 0 || mm > G.NZ) ? INF : tr.ta + (G.pz[mm] - tr.za) * tr.rcot;
     };
     double tzn = plane(m);
     int64_t k = 0;
@@ -434,11 +494,21 @@ cudaError_t launch_trace_bound(const moc_geometry_t *g, const moc_track_t *tr, i
     return scan_inclusive(bnd + 1, T, scratch, st);
 }
 
-cudaError_t launch_trace_walk(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
-                              const int64_t *bnd, int64_t *off, int64_t *scratch, int32_t *sreg,
-                              uint8_t *sitv, float *sds, int32_t *err, cudaStream_t st)
+int64_t trace_table_len(const moc_geometry_t *g) { return table_len(g); }
+
+cudaError_t launch_trace_tables(const moc_geometry_t *g, double *tab, cudaStream_t st)
 {
-    trace_walk_kernel<<<grid_tracks(T), 256, 0, st>>>(trace_geo(g), tr, T, bnd, off, sreg,
+    const int64_t n = table_len(g);
+    trace_tables_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(trace_geo(g), tab);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_walk(const moc_geometry_t *g, const double *tab, const moc_track_t *tr,
+                              int64_t T, const int64_t *bnd, int64_t *off, int64_t *scratch,
+                              int32_t *sreg, uint8_t *sitv, float *sds, int32_t *err,
+                              cudaStream_t st)
+{
+    trace_walk_kernel<<<grid_tracks(T), 256, 0, st>>>(trace_geo(g, tab), tr, T, bnd, off, sreg,
                                                        sitv, sds, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -458,12 +528,12 @@ cudaError_t launch_trace_compact(const moc_track_t *tr, int64_t T, const int64_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace_emit(const moc_geometry_t *g, const moc_track_t *tr, int64_t T,
-                              const int64_t *off, int32_t *reg, uint8_t *itv, float *ds,
-                              int32_t *err, cudaStream_t st)
+cudaError_t launch_trace_emit(const moc_geometry_t *g, const double *tab, const moc_track_t *tr,
+                              int64_t T, const int64_t *off, int32_t *reg, uint8_t *itv,
+                              float *ds, int32_t *err, cudaStream_t st)
 {
     if (T == 0) return cudaSuccess;
-    const TraceGeo G = trace_geo(g);
+    const TraceGeo G = trace_geo(g, tab);
     trace_emit_kernel<<<grid_tracks(T), 256, 0, st>>>(G, tr, T, off, reg, itv, ds, err);
     return cudaGetLastError();
 }
