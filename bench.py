@@ -16,6 +16,10 @@ no dataset; it draws random inputs itself).
                tally reductions), with the HBM fraction beside it
   cpu_baseline the reference sweep restated in C (OpenMP over tracks, per-cell locks,
                the reference's gnu flags), on a bounded sample of the same workload
+  forms        the precision, batching and differentiation forms beside the plain sweep
+  tracks       track generation (the step before the sweep): ray tracing a 17 x 17
+               assembly into 58.5M segment descriptors, segments/s, with the oracle's
+               CPU tracer timed beside it
 
 --impl reference times that CPU reference arm alone (all host threads), as the
 reference's own path for this workload.
@@ -356,6 +360,8 @@ def gpu_arm(args, workload):
     }
     if not args.no_forms and ws == 1:
         line["forms"] = forms_section(h, dp, hp, sweep_s * 1e3)
+    if not args.no_tracks and ws == 1:
+        line["tracks"] = tracks_section(h)
     if not args.no_cpu_baseline and ws == 1:
         r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
                          args.table_points if args.exp == "table" else 0)
@@ -492,6 +498,92 @@ def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
     return out
 
 
+# Track generation (include/moc_tracks.h): a 17 x 17 assembly 200 cm tall, 3 fuel rings,
+# 40 axial source regions of 5 fine intervals; 8 azimuths x 4 polar bins, 0.1 cm radial
+# and 2 cm axial track spacing: 747,024 tracks, 58.5M segments.
+TRACKS_GEOMETRY = dict(nx=17, ny=17, n_rings=3, n_axial=40, n_intervals=5, pitch=1.26,
+                       fuel_radius=0.54, height=200.0)
+TRACKS_QUADRATURE = dict(n_azim=8, n_polar=4, spacing=0.1, axial_spacing=2.0)
+# FP64 arithmetic instructions per segment of the walk (DADD 11.49 + DMUL 12.52 + DFMA
+# 1.67, thread level), from ncu's instruction counters on this workload
+# (profiles/trace_walk_assembly_58M_ncu.md). The FP64 pipe issues one of them per slot
+# whatever its kind, so the peak is the measured DFMA instruction rate.
+TRACE_FP64_INST_PER_SEGMENT = 25.68
+
+
+def tracks_section(h, reps: int = 5) -> dict:
+    """moc_trace_count + moc_trace_segments on the assembly workload, CUDA events around
+    the pair (their host synchronisations included), median of reps after one warm-up;
+    the oracle's OpenMP tracer timed on this host beside it."""
+    import numpy as np
+    import torch
+
+    import mocatt
+
+    g = mocatt.geometry(**TRACKS_GEOMETRY)
+    q = mocatt.quadrature(**TRACKS_QUADRATURE)
+    plan = mocatt.tracks_plan(g, q)
+    T = len(plan)
+    d = torch.from_numpy(plan.view(np.uint8)).cuda()
+    off, reg, itv, ds = h.trace(g, d, T)
+    if h.synchronize():
+        raise RuntimeError("device error in track generation")
+    S = int(off[-1].item())
+    L = mocatt.lib()
+    st = torch.cuda.current_stream()
+    n = C.c_int64()
+    ts = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        h.check(L.moc_trace_count(h.ptr, C.byref(g), d.data_ptr(), T, off.data_ptr(),
+                                  C.byref(n), C.c_void_p(st.cuda_stream)))
+        h.check(L.moc_trace_segments(h.ptr, C.byref(g), d.data_ptr(), T, off.data_ptr(),
+                                     reg.data_ptr(), itv.data_ptr(), ds.data_ptr(),
+                                     C.c_void_p(st.cuda_stream)))
+        e1.record(st)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    if h.synchronize() or n.value != S:
+        raise RuntimeError("track generation changed between calls")
+    ms = float(np.median(ts))
+    out = {"workload": "assembly_17x17_58M", "geometry": TRACKS_GEOMETRY,
+           "quadrature": TRACKS_QUADRATURE, "tracks": T, "segments": S,
+           "ms": ms, "value": S / (ms * 1e-3), "unit": "segments/s",
+           "timed": "moc_trace_count + moc_trace_segments (bounds, one walk, scans, "
+                    "compaction, two host synchronisations), CUDA events, median of "
+                    f"{reps} after 1 warm-up",
+           "parity": "bit for bit against the oracle's sort-all-crossings tracer "
+                     "(tests/test_tracks_gpu.py)"}
+    peaks = load_peaks()
+    if peaks.get("fp64_fma_tflops"):
+        ach = TRACE_FP64_INST_PER_SEGMENT * S / (ms * 1e-3) / 1e9
+        peak = peaks["fp64_fma_tflops"] * 1e3 / 2  # DFMA instructions per second
+        out["roofline"] = {"bound": "fp64 pipe", "unit": "G FP64 instructions/s",
+                           "achieved": ach, "peak": peak, "frac": ach / peak,
+                           "inst_per_segment": TRACE_FP64_INST_PER_SEGMENT,
+                           "peak_source": "profiles/peaks_gb300.json fp64_fma_tflops / 2 "
+                                          "(bench.py --peaks, csrc/moc_peaks.cu)",
+                           "time": "the whole timed pair, not the walk kernel alone"}
+    # the CPU arm: the oracle (test infrastructure), here only as the timed baseline
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    threads = os.cpu_count() or 1
+    oracle.trace_count_omp(g, plan[: min(T, 20000)], threads)  # warm-up
+    t0 = time.perf_counter()
+    n_cpu = oracle.trace_count_omp(g, plan, threads)
+    cpu_s = time.perf_counter() - t0
+    if n_cpu != S:
+        raise RuntimeError(f"oracle counts {n_cpu} segments, the GPU {S}")
+    out["cpu_baseline"] = {"value": S / cpu_s, "unit": "segments/s", "cores": threads,
+                           "kind": "port",
+                           "sample": "the whole plan (the reference has no tracer: the "
+                                     "oracle's tracer, OpenMP over tracks, counting)"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -504,6 +596,8 @@ def main():
     ap.add_argument("--cpu-sample-tracks", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--no-tracks", action="store_true",
+                    help="skip the track-generation line")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the precision / adjoint / batching measurements")
     ap.add_argument("--segments", type=int, default=0,
