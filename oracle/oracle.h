@@ -101,6 +101,21 @@ int64_t oracle_trace(const moc_geometry_t *g, const moc_track_t *tracks, int64_t
 int64_t oracle_trace_omp(const moc_geometry_t *g, const moc_track_t *tracks,
                          int64_t n_tracks, int nthreads);
 
+/* Source update (include/moc_transport.h), oracle/transport.c. Cross sections as host
+ * arrays in moc_xs_t's layout. FP32: every source value the same fmaf chain, in the same
+ * order, as the GPU kernel; fission = sum over cells (in cell order) of F V. FP64: the
+ * same definition in double from double tallies. Return 0, or -1 on invalid input. */
+int oracle_source_update_fp32(int32_t M, int32_t G, int32_t Gs, const float *scatter,
+                              const float *nu_fission, const float *chi,
+                              const int32_t *material, int32_t R, int32_t I,
+                              const double *volume, const float *tally, double k,
+                              float *source, double *fission);
+int oracle_source_update_fp64(int32_t M, int32_t G, int32_t Gs, const float *scatter,
+                              const float *nu_fission, const float *chi,
+                              const int32_t *material, int32_t R, int32_t I,
+                              const double *volume, const double *tally, double k,
+                              double *source, double *fission);
+
 #ifdef __cplusplus
 }
 #endif

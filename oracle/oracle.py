@@ -41,6 +41,12 @@ _SIGS = {
     "oracle_trace": (C.c_int64, [C.POINTER(mocatt.MocGeometry), _P, C.c_int64, _P, _P, _P,
                                  _P, C.c_int64]),
     "oracle_trace_omp": (C.c_int64, [C.POINTER(mocatt.MocGeometry), _P, C.c_int64, C.c_int]),
+    "oracle_source_update_fp32": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P,
+                                            C.c_int32, C.c_int32, _P, _P, C.c_double, _P,
+                                            C.POINTER(C.c_double)]),
+    "oracle_source_update_fp64": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P,
+                                            C.c_int32, C.c_int32, _P, _P, C.c_double, _P,
+                                            C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -272,3 +278,51 @@ def trace_count_omp(g, tracks: np.ndarray, nthreads: int = 0) -> int:
     tracks = np.ascontiguousarray(tracks, mocatt.TRACK_DTYPE)
     return int(lib().oracle_trace_omp(C.byref(g), tracks.ctypes.data if len(tracks) else None,
                                       len(tracks), nthreads))
+
+
+# ---- source update and power iteration ---------------------------------------------------
+
+def source_update(xs, material, R, I, volume, tally, k, fp64=False):
+    """The oracle's source update. xs: mocatt.HostXS; tally float32 [R*I, Gs] (float64 for
+    fp64). Returns (source, fission total)."""
+    L = lib()
+    material = np.ascontiguousarray(material, np.int32)
+    volume = np.ascontiguousarray(volume, np.float64)
+    fis = C.c_double()
+    if fp64:
+        tally = np.ascontiguousarray(tally, np.float64)
+        out = np.zeros(tally.shape, np.float64)
+        fn = L.oracle_source_update_fp64
+    else:
+        tally = np.ascontiguousarray(tally, np.float32)
+        out = np.zeros(tally.shape, np.float32)
+        fn = L.oracle_source_update_fp32
+    st = fn(xs.M, xs.G, xs.Gs, xs.scatter.ctypes.data, xs.nu_fission.ctypes.data,
+            xs.chi.ctypes.data, material.ctypes.data, R, I, volume.ctypes.data,
+            tally.ctypes.data, float(k), out.ctypes.data, C.byref(fis))
+    if st:
+        raise ValueError("invalid source update input")
+    return out, fis.value
+
+
+def power_iteration(hp, opts, xs, material, volume, k, iterations):
+    """moc_power_iteration restated: the FP32 sweep oracle (oracle_fwd_fp32) and the FP32
+    source update, vacuum boundaries. hp: mocatt.HostProblem whose fine_flux holds the
+    starting tallies and whose sigT is the materials'; updated in place. Returns the
+    eigenvalue after each iteration."""
+    src, F_prev = source_update(xs, material, hp.R, hp.I, volume, hp.fine_flux, k)
+    hp.source[:] = src
+    ks = []
+    for _ in range(iterations):
+        hp.psi[:] = 0
+        hp.fine_flux[:] = 0
+        psi, ff = fwd_fp32(hp, opts)
+        hp.psi[:] = psi
+        hp.fine_flux[:] = ff
+        src, F = source_update(xs, material, hp.R, hp.I, volume, hp.fine_flux, k)
+        hp.source[:] = src
+        k = k * F / F_prev
+        F_prev = F
+        ks.append(k)
+    return ks
+

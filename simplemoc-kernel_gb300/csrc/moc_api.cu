@@ -67,6 +67,8 @@ struct moc_handle_s {
     size_t tscan_cap = 0, tbnd_cap = 0;
     double *ttab = nullptr;              // the walk's tables of the geometry
     size_t ttab_cap = 0;
+    double *fis = nullptr;               // power iteration: the fission total
+    size_t fis_cap = 0;
     int32_t *treg = nullptr;
     uint8_t *titv = nullptr;
     float *tds = nullptr;
@@ -928,6 +930,7 @@ moc_status_t moc_destroy(moc_handle_t h)
     if (h->tscan) cudaFree(h->tscan);
     if (h->tbnd) cudaFree(h->tbnd);
     if (h->ttab) cudaFree(h->ttab);
+    if (h->fis) cudaFree(h->fis);
     if (h->treg) cudaFree(h->treg);
     if (h->titv) cudaFree(h->titv);
     if (h->tds) cudaFree(h->tds);
@@ -1479,6 +1482,114 @@ moc_status_t moc_trace_segments(moc_handle_t h, const moc_geometry_t *g,
     MOC_CUDA(h, moc::launch_trace_emit(g, h->ttab, d_tracks, n_tracks, d_track_offsets,
                                        d_seg_region, d_seg_interval, d_seg_ds, h->err, st));
     return MOC_OK;
+}
+
+// ---- source update and power iteration (include/moc_transport.h; moc_transport.cu) ----
+
+bool xs_ok(const moc_xs_t *xs)
+{
+    return xs && xs->n_materials >= 1 && xs->n_groups >= 1 && xs->n_groups <= 256 &&
+           xs->group_stride >= xs->n_groups && xs->group_stride % 4 == 0 && xs->sigT &&
+           xs->scatter && xs->nu_fission && xs->chi && aligned(xs->sigT, 16) &&
+           aligned(xs->scatter, 16) && aligned(xs->nu_fission, 16) && aligned(xs->chi, 16);
+}
+
+moc_status_t moc_region_sigT(moc_handle_t h, const moc_xs_t *xs, const int32_t *material,
+                             int32_t n_regions, float *sigT, void *stream)
+{
+    if (!h || !xs_ok(xs) || n_regions < 0 || (n_regions > 0 && (!material || !sigT)))
+        return MOC_ERR_INVALID_ARG;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    MOC_CUDA(h, moc::launch_region_sigT(xs, material, n_regions, sigT, h->err,
+                                        static_cast<cudaStream_t>(stream)));
+    return MOC_OK;
+}
+
+moc_status_t source_update(moc_handle_t h, const moc_xs_t *xs, const int32_t *material,
+                           int32_t R, int32_t I, const double *volume, const float *fine_flux,
+                           double k, float *source, double *fission, cudaStream_t st)
+{
+    moc::TransportParams P;
+    P.ncell = (int64_t)R * I;
+    P.M = xs->n_materials;
+    P.G = xs->n_groups;
+    P.Gs = xs->group_stride;
+    P.I = I;
+    P.scatter = xs->scatter;
+    P.nu_fission = xs->nu_fission;
+    P.chi = xs->chi;
+    P.rk = (float)(1.0 / k);
+    P.rpi = (float)(1.0 / (4.0 * 3.14159265358979323846));
+    MOC_CUDA(h, moc::launch_source_update(P, material, volume, fine_flux, source, fission,
+                                          h->err, st));
+    return MOC_OK;
+}
+
+moc_status_t moc_source_update(moc_handle_t h, const moc_xs_t *xs, const int32_t *material,
+                               int32_t n_regions, int32_t n_intervals, const double *volume,
+                               const float *fine_flux, double k, float *source,
+                               double *fission, void *stream)
+{
+    if (!h || !xs_ok(xs) || n_regions < 0 || n_intervals < 1 || !(k > 0.0) ||
+        (n_regions > 0 && (!material || !volume || !fine_flux || !source || !fission)))
+        return MOC_ERR_INVALID_ARG;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    return source_update(h, xs, material, n_regions, n_intervals, volume, fine_flux, k, source,
+                         fission, static_cast<cudaStream_t>(stream));
+}
+
+moc_status_t moc_power_iteration(moc_handle_t h, const moc_problem_t *p,
+                                 const moc_fwd_opts_t *opts, const moc_xs_t *xs,
+                                 const int32_t *material, const double *volume,
+                                 const moc_eigen_opts_t *eo, double *k, int32_t *iterations,
+                                 void *stream)
+{
+    if (!h || !p || !opts || !xs_ok(xs) || !material || !volume || !eo || !k || !iterations ||
+        !(*k > 0.0) || eo->max_iterations < 1 || !(eo->tolerance >= 0.0) ||
+        xs->n_groups != p->n_groups || xs->group_stride != p->group_stride)
+        return MOC_ERR_INVALID_ARG;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    moc_status_t s;
+    if ((s = ensure(h, reinterpret_cast<void **>(&h->fis), &h->fis_cap, sizeof(double))))
+        return s;
+    const int32_t R = p->n_regions, I = p->n_intervals;
+    const size_t nff = (size_t)R * I * p->group_stride;
+    const size_t npsi = (size_t)p->n_tracks * p->group_stride;
+    auto update = [&](double kk, double *F) -> moc_status_t {
+        MOC_CUDA(h, cudaMemsetAsync(h->fis, 0, sizeof(double), st));
+        // the problem's source is this call's workspace (see the header)
+        moc_status_t s2 = source_update(h, xs, material, R, I, volume, p->fine_flux, kk,
+                                        const_cast<float *>(p->source), h->fis, st);
+        if (s2) return s2;
+        MOC_CUDA(h, cudaMemcpyAsync(F, h->fis, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MOC_CUDA(h, cudaStreamSynchronize(st));
+        return MOC_OK;
+    };
+    double kk = *k, F_prev = 0.0;
+    if ((s = update(kk, &F_prev))) return s;
+    int32_t it = 0;
+    while (it < eo->max_iterations) {
+        MOC_CUDA(h, cudaMemsetAsync(p->psi, 0, npsi * sizeof(float), st));
+        MOC_CUDA(h, cudaMemsetAsync(p->fine_flux, 0, nff * sizeof(float), st));
+        if ((s = moc_attenuate_fwd(h, p, opts, stream))) return s;
+        double F = 0.0;
+        if ((s = update(kk, &F))) return s;
+        it++;
+        if (!(F_prev > 0.0) || !(F >= 0.0)) {  // no fission source: nothing to normalise
+            *k = kk;
+            *iterations = it;
+            return MOC_ERR_INVALID_ARG;
+        }
+        const double kn = kk * F / F_prev;
+        const bool done = std::fabs(kn - kk) <= eo->tolerance * kn;
+        kk = kn;
+        F_prev = F;
+        if (done) break;
+    }
+    *k = kk;
+    *iterations = it;
+    return moc_synchronize(h, stream);
 }
 
 moc_status_t moc_build_exp_table(int32_t n_points, float max_val, float *values, float *dx,

@@ -6,6 +6,7 @@
 
 #include "moc_attenuate.h"
 #include "moc_tracks.h"
+#include "moc_transport.h"
 
 // Two groups' FP32 arithmetic per packed .f32x2 instruction where a lane of the sweep holds
 // an even number of groups (bit-identical to the one-group form; -DMOC_PAIRED_FP32=0
@@ -274,5 +275,18 @@ cudaError_t launch_trace_compact(const moc_track_t *tr, int64_t T, const int64_t
 cudaError_t launch_trace_emit(const moc_geometry_t *g, const double *tab, const moc_track_t *tr,
                               int64_t T, const int64_t *off, int32_t *reg, uint8_t *itv,
                               float *ds, int32_t *err, cudaStream_t st);
+
+// Source update (moc_transport.cu). rk = (float)(1 / k), rpi = (float)(1 / (4 pi)).
+struct TransportParams {
+    int64_t ncell;  // R * I fine cells
+    int M, G, Gs, I;
+    const float *scatter, *nu_fission, *chi;
+    float rk, rpi;
+};
+cudaError_t launch_region_sigT(const moc_xs_t *xs, const int32_t *material, int64_t R,
+                               float *sigT, int32_t *err, cudaStream_t st);
+cudaError_t launch_source_update(const TransportParams &P, const int32_t *material,
+                                 const double *volume, const float *tally, float *source,
+                                 double *fission, int32_t *err, cudaStream_t st);
 
 }  // namespace moc

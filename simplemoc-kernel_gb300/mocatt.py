@@ -96,6 +96,20 @@ class MocQuadrature(C.Structure):
                 ("spacing", C.c_double), ("axial_spacing", C.c_double)]
 
 
+class MocXS(C.Structure):
+    """moc_xs_t (include/moc_transport.h)."""
+    _fields_ = [("n_materials", C.c_int32), ("n_groups", C.c_int32),
+                ("group_stride", C.c_int32), ("reserved", C.c_int32),
+                ("sigT", C.c_void_p), ("scatter", C.c_void_p), ("nu_fission", C.c_void_p),
+                ("chi", C.c_void_p)]
+
+
+class MocEigenOpts(C.Structure):
+    """moc_eigen_opts_t (include/moc_transport.h)."""
+    _fields_ = [("max_iterations", C.c_int32), ("reserved", C.c_int32),
+                ("tolerance", C.c_double)]
+
+
 # moc_track_t as a numpy record (112 bytes)
 TRACK_DTYPE = np.dtype([(n, np.float64) for n in (
     "x0", "y0", "ux", "uy", "rux", "ruy", "ta", "tb", "za", "cot", "rcot", "rsin")] +
@@ -145,6 +159,12 @@ ABI = {
                                   C.POINTER(C.c_int64), _P]),
     "moc_trace_segments": (C.c_int, [_P, C.POINTER(MocGeometry), _P, C.c_int64, _P, _P,
                                      _P, _P, _P]),
+    "moc_region_sigT": (C.c_int, [_P, C.POINTER(MocXS), _P, C.c_int32, _P, _P]),
+    "moc_source_update": (C.c_int, [_P, C.POINTER(MocXS), _P, C.c_int32, C.c_int32, _P, _P,
+                                    C.c_double, _P, _P, _P]),
+    "moc_power_iteration": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts),
+                                      C.POINTER(MocXS), _P, _P, C.POINTER(MocEigenOpts),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_int32), _P]),
 }
 SYNTH_ABI = {
     "moc_synth_spec_init": (None, [C.POINTER(SynthSpec), C.c_uint64, C.c_int32, C.c_int32,
@@ -440,6 +460,99 @@ def tracks_weight(q: MocQuadrature) -> float:
     return float(lib().moc_tracks_weight(C.byref(q)))
 
 
+# ---- cross sections (include/moc_transport.h) ---------------------------------------------
+
+@dataclasses.dataclass
+class HostXS:
+    """Multigroup cross sections of M materials in moc_xs_t's layout (host, float32)."""
+    M: int
+    G: int
+    Gs: int
+    sigT: np.ndarray        # [M, Gs]
+    scatter: np.ndarray     # [M, G, Gs]: from group g' (axis 1) into group g (axis 2)
+    nu_fission: np.ndarray  # [M, Gs]
+    chi: np.ndarray         # [M, Gs]
+
+
+def synth_xs(M: int, G: int, seed: int = 7, fissile=None) -> HostXS:
+    """Seeded synthetic cross sections: material 0 a scatterer (scattering ratio ~0.9,
+    no fission), the others fissile (~0.5, nu_fission ~1.6 x absorption); total cross
+    sections rising with the group index (fast to thermal), scattering mostly into the
+    same and lower-energy groups with some up-scattering in the last quarter, and chi
+    over the first third of the groups, normalised."""
+    rng = np.random.default_rng(seed)
+    Gs = (G + 3) & ~3
+    fissile = set(range(1, M)) if fissile is None else set(fissile)
+    sig = _aligned_empty((M, Gs), np.float32)
+    sc = _aligned_empty((M, G, Gs), np.float32)
+    nuf = _aligned_empty((M, Gs), np.float32)
+    chi = _aligned_empty((M, Gs), np.float32)
+    for a in (sig, sc, nuf, chi):
+        a[:] = 0
+    gg = np.arange(G)
+    for m in range(M):
+        st = 0.25 + 1.2 * gg / max(G - 1, 1) + 0.05 * rng.random(G)
+        ratio = 0.9 if m not in fissile else 0.5
+        w = rng.random((G, G)) + 0.05
+        down = gg[None, :] >= gg[:, None]                 # g >= g'
+        up = (gg[:, None] >= 3 * G // 4) & (gg[None, :] >= 3 * G // 4)
+        w = np.where(down | up, w, 0.0)
+        w /= w.sum(axis=1, keepdims=True)
+        sig[m, :G] = st
+        sc[m, :, :G] = (ratio * st)[:, None] * w
+        if m in fissile:
+            nuf[m, :G] = 1.6 * (1.0 - ratio) * st
+            c = np.where(gg < max(1, G // 3), rng.random(G) + 0.1, 0.0)
+            chi[m, :G] = c / c.sum()
+    return HostXS(M, G, Gs, sig, sc, nuf, chi)
+
+
+def geometry_materials(g) -> np.ndarray:
+    """Material of every region of a traced geometry (include/moc_tracks.h numbering):
+    moderator 0, fuel ring k material 1 + k."""
+    R = geometry_regions(g)
+    ring = (np.arange(R) // g.n_axial) % (g.n_rings + 1)
+    return np.where(ring == g.n_rings, 0, 1 + ring).astype(np.int32)
+
+
+def problem_from_tracks(g, off, reg, itv, ds, xs: HostXS):
+    """A host problem on traced descriptors (int64 offsets, int32 regions, uint8
+    intervals, float32 lengths) of geometry g with the materials' sigT, a zero source and
+    psi, and fine_flux = the cell volumes in every group (the starting tallies of a flat
+    flux phi = 1). Returns (problem, material [R] int32, volume [R*I] float64)."""
+    R, I = geometry_regions(g), g.n_intervals
+    T = len(off) - 1
+    mat = geometry_materials(g)
+    vol = geometry_volumes(g)
+    sig = _aligned_empty((R, xs.Gs), np.float32)
+    sig[:] = xs.sigT[mat]
+    src = _aligned_empty((R * I, xs.Gs), np.float32)
+    src[:] = 0
+    ff = _aligned_empty((R * I, xs.Gs), np.float32)
+    ff[:] = 0
+    ff[:, :xs.G] = vol[:, None].astype(np.float32)
+    psi = _aligned_empty((T, xs.Gs), np.float32)
+    psi[:] = 0
+    hp = HostProblem(R, I, xs.G, xs.Gs, T, int(off[-1]), np.ascontiguousarray(off, np.int64),
+                     np.ascontiguousarray(reg, np.int32), np.ascontiguousarray(itv, np.uint8),
+                     np.ascontiguousarray(ds, np.float32), sig, src, ff, psi)
+    return hp, mat, vol
+
+
+class DeviceXS:
+    """HostXS on the GPU and its moc_xs_t."""
+
+    def __init__(self, xs: HostXS, device="cuda:0"):
+        import torch
+        self.M, self.G, self.Gs = xs.M, xs.G, xs.Gs
+        for n in ("sigT", "scatter", "nu_fission", "chi"):
+            setattr(self, n, torch.from_numpy(np.ascontiguousarray(getattr(xs, n))).to(device))
+
+    def c_struct(self) -> MocXS:
+        return MocXS(self.M, self.G, self.Gs, 0, self.sigT.data_ptr(), self.scatter.data_ptr(),
+                     self.nu_fission.data_ptr(), self.chi.data_ptr())
+
+
 class DeviceProblem:
     """A problem resident on the GPU (torch tensors), and its C struct."""
 
@@ -454,6 +567,16 @@ class DeviceProblem:
             t = torch.from_numpy(np.ascontiguousarray(a)).to(device) if a.size else \
                 torch.empty(max(1, a.size), dtype=torch.from_numpy(a).dtype, device=device)
             setattr(self, n, t)
+
+    @classmethod
+    def from_tensors(cls, R, I, G, Gs, T, S, **tensors) -> "DeviceProblem":
+        """A device problem over existing device tensors (e.g. traced descriptors), one
+        per name of NAMES."""
+        dp = cls.__new__(cls)
+        dp.R, dp.I, dp.G, dp.Gs, dp.T, dp.S = R, I, G, Gs, T, S
+        for n in cls.NAMES:
+            setattr(dp, n, tensors[n])
+        return dp
 
     def c_struct(self) -> MocProblem:
         return MocProblem(self.R, self.I, self.G, self.Gs, self.T, 0, self.S,
@@ -529,6 +652,49 @@ class Handle:
                                         off.data_ptr(), reg.data_ptr(), itv.data_ptr(),
                                         ds.data_ptr(), C.c_void_p(s.cuda_stream)))
         return off, reg[:n], itv[:n], ds[:n]
+
+    def region_sigT(self, xs: DeviceXS, material, stream=None):
+        """moc_region_sigT: the regions' sigT [R, Gs] from their materials (device)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        R = material.numel()
+        out = torch.empty((R, xs.Gs), dtype=torch.float32, device=material.device)
+        xc = xs.c_struct()
+        self.check(lib().moc_region_sigT(self._h, C.byref(xc), material.data_ptr(), R,
+                                         out.data_ptr(), C.c_void_p(s.cuda_stream)))
+        return out
+
+    def source_update(self, xs: DeviceXS, material, I: int, volume, tally, k: float,
+                      stream=None):
+        """moc_source_update: returns (source [R*I, Gs] device tensor, fission total)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        src = torch.zeros_like(tally)
+        fis = torch.zeros(1, dtype=torch.float64, device=tally.device)
+        xc = xs.c_struct()
+        self.check(lib().moc_source_update(self._h, C.byref(xc), material.data_ptr(),
+                                           material.numel(), I, volume.data_ptr(),
+                                           tally.data_ptr(), float(k), src.data_ptr(),
+                                           fis.data_ptr(), C.c_void_p(s.cuda_stream)))
+        return src, fis
+
+    def power_iteration(self, dp: "DeviceProblem", opts: MocFwdOpts, xs: DeviceXS, material,
+                        volume, k: float, max_iterations: int, tolerance: float = 0.0,
+                        stream=None):
+        """moc_power_iteration on dp (its fine_flux the starting tallies). Returns
+        (k, iterations)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        kk = C.c_double(k)
+        it = C.c_int32()
+        eo = MocEigenOpts(max_iterations, 0, tolerance)
+        prob = dp.c_struct()
+        xc = xs.c_struct()
+        self.check(lib().moc_power_iteration(self._h, C.byref(prob), C.byref(opts), C.byref(xc),
+                                             material.data_ptr(), volume.data_ptr(),
+                                             C.byref(eo), C.byref(kk), C.byref(it),
+                                             C.c_void_p(s.cuda_stream)))
+        return kk.value, it.value
 
     def fwd_host(self, hp: HostProblem, opts: MocFwdOpts | None = None):
         opts = opts or default_opts()

@@ -30,10 +30,10 @@ NVCC_FLAGS = ARCH + [
     "-I" + INCLUDE, "-I" + CSRC,
 ]
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu", "moc_adjoint.cu",
-              "moc_batch.cu", "moc_split.cu", "moc_trace.cu"]
+              "moc_batch.cu", "moc_split.cu", "moc_trace.cu", "moc_transport.cu"]
 # Per-file flags: the track walk rounds every FP64 operation on its own, as the C oracle
 # compiled with -ffp-contract=off does, so its descriptors match the oracle's bit for bit.
-EXTRA_FLAGS = {"moc_trace.cu": ["-fmad=false"]}
+EXTRA_FLAGS = {"moc_trace.cu": ["-fmad=false"], "moc_transport.cu": ["-fmad=false"]}
 
 LIB = os.path.join(BUILD, "libmocatt.so")
 SYNTH_LIB = os.path.join(BUILD, "libmocsynth.so")
