@@ -20,6 +20,9 @@ no dataset; it draws random inputs itself).
   tracks       track generation (the step before the sweep): ray tracing a 17 x 17
                assembly into 58.5M segment descriptors, segments/s, with the oracle's
                CPU tracer timed beside it
+  transport    the power iteration around the sweep (the step after): the traced
+               assembly swept both ways at 128 groups, source update and eigenvalue,
+               time per iteration, with the oracle's source update timed beside it
 
 --impl reference times that CPU reference arm alone (all host threads), as the
 reference's own path for this workload.
@@ -362,6 +365,7 @@ def gpu_arm(args, workload):
         line["forms"] = forms_section(h, dp, hp, sweep_s * 1e3)
     if not args.no_tracks and ws == 1:
         line["tracks"] = tracks_section(h)
+        line["transport"] = transport_section(h)
     if not args.no_cpu_baseline and ws == 1:
         r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
                          args.table_points if args.exp == "table" else 0)
@@ -581,6 +585,93 @@ def tracks_section(h, reps: int = 5) -> dict:
                            "kind": "port",
                            "sample": "the whole plan (the reference has no tracer: the "
                                      "oracle's tracer, OpenMP over tracks, counting)"}
+    return out
+
+
+def transport_section(h, iterations: int = 10) -> dict:
+    """The power iteration around the sweep (include/moc_transport.h) on the traced
+    assembly, both directions, 128 groups, 4 synthetic materials, flat sources, vacuum
+    boundaries: moc_power_iteration timed with CUDA events (its per-iteration host
+    synchronisation included) after 2 warm-up iterations; the sweep and the source update
+    timed apart; the oracle's FP32 source update timed on this host beside it."""
+    import numpy as np
+    import torch
+
+    import mocatt
+
+    G = 128
+    g = mocatt.geometry(**TRACKS_GEOMETRY)
+    q = mocatt.quadrature(both_directions=1, **TRACKS_QUADRATURE)
+    plan = mocatt.tracks_plan(g, q)
+    d = torch.from_numpy(plan.view(np.uint8)).cuda()
+    off, reg, itv, ds = h.trace(g, d, len(plan))
+    T, S = len(plan), int(off[-1].item())
+    R, I = mocatt.geometry_regions(g), g.n_intervals
+    xs = mocatt.synth_xs(4, G)
+    dxs = mocatt.DeviceXS(xs)
+    mat = mocatt.geometry_materials(g)
+    vol = mocatt.geometry_volumes(g)
+    dmat, dvol = torch.from_numpy(mat).cuda(), torch.from_numpy(vol).cuda()
+    ff = torch.zeros((R * I, xs.Gs), device="cuda")
+    ff[:, :G] = dvol[:, None].float()
+    dp = mocatt.DeviceProblem.from_tensors(
+        R, I, G, xs.Gs, T, S, track_offsets=off, seg_region=reg, seg_interval=itv, seg_ds=ds,
+        sigT=h.region_sigT(dxs, dmat), source=torch.zeros_like(ff), fine_flux=ff,
+        psi=torch.zeros((T, xs.Gs), device="cuda"))
+    opts = mocatt.default_opts(weight=mocatt.tracks_weight(q), zin=0.0, mu=0.0, mu2=0.0)
+    k, _ = h.power_iteration(dp, opts, dxs, dmat, dvol, 1.0, 2)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    k, it = h.power_iteration(dp, opts, dxs, dmat, dvol, k, iterations)
+    e1.record(st)
+    e1.synchronize()
+    ms_it = e0.elapsed_time(e1) / it
+    popts = mocatt.default_opts(weight=mocatt.tracks_weight(q), zin=0.0, mu=0.0, mu2=0.0,
+                                profile=1)
+    sweep = _time_fwd(h, dp, popts)
+    e0.record(st)
+    for _ in range(5):
+        h.source_update(dxs, dmat, I, dvol, dp.fine_flux, k)
+    e1.record(st)
+    e1.synchronize()
+    upd_ms = e0.elapsed_time(e1) / 5
+    if h.synchronize():
+        raise RuntimeError("device error in the power iteration")
+    cells = R * I
+    flops = 2.0 * G * (G + 1) * cells  # the scattering and fission chains
+    peaks = load_peaks()
+    out = {"workload": "assembly_17x17_both_directions_g128", "tracks": T, "segments": S,
+           "groups": G, "cells": cells, "materials": xs.M, "iterations": it, "k": k,
+           "ms_per_iteration": ms_it, "value": 1e3 / ms_it, "unit": "power iterations/s",
+           "attenuations_per_s": S * G / (ms_it * 1e-3),
+           "sweep_ms": sweep, "source_update_ms": upd_ms,
+           "timed": "moc_power_iteration over the iterations (psi and tally resets, sweep, "
+                    "source update, one host synchronisation each), CUDA events",
+           "parity": "source update bit for bit against the oracle's FP32 restatement; "
+                     "iteration against the oracle's (tests/test_transport_gpu.py)"}
+    if peaks.get("fp32_fma_tflops"):
+        ach = flops / (upd_ms * 1e-3) / 1e12
+        out["source_update_roofline"] = {
+            "bound": "fp32", "unit": "TFLOP/s", "achieved": ach,
+            "peak": peaks["fp32_fma_tflops"], "frac": ach / peaks["fp32_fma_tflops"],
+            "flops_per_cell": 2.0 * G * (G + 1),
+            "peak_source": "profiles/peaks_gb300.json fp32_fma_tflops"}
+    # the CPU arm: the oracle's source update (test infrastructure), one thread, on the
+    # first 20,000 cells of the same tallies
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    n = min(cells, 20000)
+    nreg = (n + I - 1) // I
+    tally = dp.fine_flux[: nreg * I].cpu().numpy()
+    t0 = time.perf_counter()
+    oracle.source_update(xs, mat[:nreg], nreg, I, vol[: nreg * I], tally, k)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": nreg * I / cpu_s, "unit": "cells/s (source update)",
+                           "gpu_value": cells / (upd_ms * 1e-3), "cores": 1, "kind": "port",
+                           "sample": f"the oracle's FP32 source update of the first "
+                                     f"{nreg * I} of {cells} cells, 128 groups"}
     return out
 
 
