@@ -60,8 +60,10 @@ typedef enum {
     MOC_ERR_DEVICE_TIMEOUT = 8,  /* a bounded device-side wait gave up               */
     MOC_ERR_TOO_LARGE = 9,       /* the problem exceeds the fixed scratch of
                                     moc_attenuate_fwd_noalloc                         */
-    MOC_ERR_BAD_TRACK = 10       /* track generation (moc_tracks.h): a track record is
+    MOC_ERR_BAD_TRACK = 10,      /* track generation (moc_tracks.h): a track record is
                                     invalid or disagrees with the offsets             */
+    MOC_ERR_IO = 11              /* a track file (moc_trackfile.h) cannot be written or
+                                    read, or is short, corrupt or inconsistent        */
 } moc_status_t;
 
 typedef struct moc_handle_s *moc_handle_t;

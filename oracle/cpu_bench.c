@@ -15,6 +15,10 @@
  *   --ds LO HI                           ds ~ U(LO, HI) (default 0.01 1.0)
  *   --table N MAX                        table exp mode
  *   --sample-tracks K --threads N --steps K --warmup W
+ *   --track-file PATH                    the segments of a track file
+ *                                        (include/moc_trackfile.h), which sets the tracks,
+ *                                        segments, regions and intervals; tables and psi
+ *                                        stay seeded
  */
 #include "moc_synth.h"
 #include "oracle.h"
@@ -37,6 +41,7 @@ int main(int argc, char **argv)
     opts.table_max = 10.0f;
     opts.dz = 0.1f; opts.zin = 0.3f; opts.weight = 0.5f; opts.mu = 0.9f; opts.mu2 = 0.3f;
     long sample = -1;
+    const char *track_file = NULL;
     int threads = 0, steps = 3, warmup = 1;
     for (int a = 1; a < argc; a++) {
 #define ARG(name) (strcmp(argv[a], name) == 0 && a + 1 < argc)
@@ -67,17 +72,33 @@ int main(int argc, char **argv)
         else if (ARG("--threads")) threads = atoi(argv[++a]);
         else if (ARG("--steps")) steps = atoi(argv[++a]);
         else if (ARG("--warmup")) warmup = atoi(argv[++a]);
+        else if (ARG("--track-file")) track_file = argv[++a];
         else {
             fprintf(stderr, "cpu_bench: bad argument %s\n", argv[a]);
             return 2;
         }
 #undef ARG
     }
+    int64_t *foff = NULL, fT = 0, fS = 0;
+    int32_t *freg = NULL, fR = 0, fI = 0;
+    uint8_t *fitv = NULL;
+    float *fds = NULL;
+    if (track_file) {
+        if (oracle_trackfile_read(track_file, &fT, &fS, &fR, &fI, &foff, &freg, &fitv, &fds) ||
+            fT < 1 || fT > 2147483647 || fI < 2 || fI > 255) {
+            fprintf(stderr, "cpu_bench: %s is not a usable track file\n", track_file);
+            return 2;
+        }
+        spec.n_tracks = (int32_t)fT;
+        spec.n_segments = fS;
+        spec.n_regions = fR;
+        spec.n_intervals = fI;
+    }
     spec.group_stride = (spec.n_groups + 3) & ~3;
     const long T = spec.n_tracks, Gs = spec.group_stride;
     const long ncell = (long)spec.n_regions * spec.n_intervals;
-    int64_t *off = (int64_t *)malloc((size_t)(T + 1) * sizeof(int64_t));
-    const int64_t S = moc_synth_track_offsets(&spec, off);
+    int64_t *off = foff ? foff : (int64_t *)malloc((size_t)(T + 1) * sizeof(int64_t));
+    const int64_t S = foff ? fS : moc_synth_track_offsets(&spec, off);
     if (S < 0) {
         fprintf(stderr, "cpu_bench: invalid sizes\n");
         return 2;
@@ -87,14 +108,17 @@ int main(int argc, char **argv)
     float *sig = malloc((size_t)(spec.n_regions * Gs) * sizeof(float));
     float *src = malloc((size_t)(ncell * Gs) * sizeof(float));
     float *ff = calloc((size_t)(ncell * Gs), sizeof(float));
-    int32_t *reg = malloc((size_t)(S > 0 ? S : 1) * sizeof(int32_t));
-    uint8_t *itv = malloc((size_t)(S > 0 ? S : 1));
-    float *ds = malloc((size_t)(S > 0 ? S : 1) * sizeof(float));
+    int32_t *reg = freg ? freg : malloc((size_t)(S > 0 ? S : 1) * sizeof(int32_t));
+    uint8_t *itv = fitv ? fitv : malloc((size_t)(S > 0 ? S : 1));
+    float *ds = fds ? fds : malloc((size_t)(S > 0 ? S : 1) * sizeof(float));
     if (!psi0 || !psi || !sig || !src || !ff || !reg || !itv || !ds) {
         fprintf(stderr, "cpu_bench: out of memory\n");
         return 3;
     }
-    moc_synth_fill(&spec, off, psi0, sig, src, reg, itv, ds);
+    if (track_file)
+        moc_synth_fill(&spec, off, psi0, sig, src, NULL, NULL, NULL);
+    else
+        moc_synth_fill(&spec, off, psi0, sig, src, reg, itv, ds);
     if (sample < 0 || sample > T) sample = T;
 
     moc_problem_t p;

@@ -116,6 +116,13 @@ int oracle_source_update_fp64(int32_t M, int32_t G, int32_t Gs, const float *sca
                               const double *volume, const double *tally, double k,
                               double *source, double *fission);
 
+/* The on-disk track format (include/moc_trackfile.h), oracle/trackfile.c: reads a file
+ * into malloc'ed arrays (the caller frees them), checking the checksum, the offsets and
+ * the cell indices. Returns 0, or -1 for a file that is not a valid track file. */
+int oracle_trackfile_read(const char *path, int64_t *T, int64_t *S, int32_t *R, int32_t *I,
+                          int64_t **offsets, int32_t **region, uint8_t **interval,
+                          float **ds);
+
 #ifdef __cplusplus
 }
 #endif

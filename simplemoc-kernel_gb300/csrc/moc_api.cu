@@ -1650,6 +1650,7 @@ const char *moc_status_string(moc_status_t s)
     case MOC_ERR_DEVICE_TIMEOUT: return "device wait timed out";
     case MOC_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
     case MOC_ERR_BAD_TRACK: return "track record invalid or inconsistent with the offsets";
+    case MOC_ERR_IO: return "track file unwritable, unreadable, short, corrupt or inconsistent";
     }
     return "unknown status";
 }

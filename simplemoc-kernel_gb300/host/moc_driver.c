@@ -14,10 +14,15 @@
  *   -x           table exp mode with the reference's table (N = 353, maxVal = 10)
  *   -d device    CUDA device index (default 0)
  *   -n repeats   sweeps to time (default 1)
+ *   -f file      sweep the segments of a track file (include/moc_trackfile.h: its
+ *                tracks, regions and intervals replace -s, -k and -r; the tables and psi
+ *                stay seeded)
+ *   -w file      write the generated segments to a track file before sweeping
  * -t is accepted for command-line compatibility and ignored (the sweep runs on the GPU).
  */
 #include "moc_attenuate.h"
 #include "moc_synth.h"
+#include "moc_trackfile.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -41,6 +46,8 @@ static void usage(void)
            "  -x                  Use the exponential table\n"
            "  -d <device>         CUDA device\n"
            "  -n <repeats>        Sweeps to time\n"
+           "  -f <file>           Sweep the segments of a track file\n"
+           "  -w <file>           Write the generated segments to a track file\n"
            "  -t <threads>        Accepted and ignored\n");
 }
 
@@ -59,6 +66,8 @@ int main(int argc, char **argv)
     long segments = 50000000;
     int groups = 128, regions = 6750, device = 0, repeats = 1, table = 0;
     long tracks = -1;
+    int intervals = 5;
+    const char *in_file = NULL, *out_file = NULL;
     for (int i = 1; i < argc; i++) {
         const char *a = argv[i];
         const int more = i + 1 < argc;
@@ -70,22 +79,37 @@ int main(int argc, char **argv)
         else if (!strcmp(a, "-n") && more) repeats = atoi(argv[++i]);
         else if (!strcmp(a, "-t") && more) ++i;
         else if (!strcmp(a, "-x")) table = 1;
+        else if (!strcmp(a, "-f") && more) in_file = argv[++i];
+        else if (!strcmp(a, "-w") && more) out_file = argv[++i];
         else {
             usage();
             return 1;
         }
     }
+    moc_trackfile_info_t info;
+    if (in_file) {
+        const moc_status_t fs = moc_trackfile_info(in_file, &info);
+        if (fs != MOC_OK) {
+            fprintf(stderr, "%s: %s\n", in_file, moc_status_string(fs));
+            return 1;
+        }
+        segments = info.n_segments;
+        tracks = info.n_tracks;
+        regions = info.n_regions;
+        intervals = info.n_intervals;
+    }
     if (tracks < 0) tracks = segments / 500 > 0 ? segments / 500 : 1;
-    if (segments < 0 || groups < 1 || regions < 1 || tracks < 1 || repeats < 1) {
+    if (segments < 0 || groups < 1 || regions < 1 || tracks < 1 || repeats < 1 ||
+        tracks > 2147483647L) {
         usage();
         return 1;
     }
 
     moc_synth_spec_t spec;
-    moc_synth_spec_init(&spec, 1, regions, 5, groups, (int32_t)tracks, segments);
-    const long Gs = spec.group_stride, ncell = (long)regions * 5;
+    moc_synth_spec_init(&spec, 1, regions, intervals, groups, (int32_t)tracks, segments);
+    const long Gs = spec.group_stride, ncell = (long)regions * intervals;
     int64_t *off = xmalloc((size_t)(tracks + 1) * sizeof(int64_t));
-    if (moc_synth_track_offsets(&spec, off) < 0) {
+    if (!in_file && moc_synth_track_offsets(&spec, off) < 0) {
         fprintf(stderr, "invalid sizes\n");
         return 1;
     }
@@ -97,11 +121,27 @@ int main(int argc, char **argv)
     uint8_t *itv = xmalloc((size_t)segments);
     float *ds = xmalloc((size_t)segments * sizeof(float));
     if (!flux) return 3;
-    moc_synth_fill(&spec, off, psi, sigT, source, reg, itv, ds);
+    if (in_file) {
+        const moc_status_t fs = moc_trackfile_read(in_file, off, reg, itv, ds);
+        if (fs != MOC_OK || moc_synth_fill(&spec, off, psi, sigT, source, NULL, NULL, NULL)) {
+            fprintf(stderr, "%s: %s\n", in_file, moc_status_string(fs ? fs : MOC_ERR_IO));
+            return 1;
+        }
+    } else {
+        moc_synth_fill(&spec, off, psi, sigT, source, reg, itv, ds);
+    }
+    if (out_file) {
+        const moc_status_t fs = moc_trackfile_write(out_file, tracks, segments, regions,
+                                                    intervals, off, reg, itv, ds);
+        if (fs != MOC_OK) {
+            fprintf(stderr, "%s: %s\n", out_file, moc_status_string(fs));
+            return 1;
+        }
+    }
 
     moc_problem_t p = {0};
     p.n_regions = regions;
-    p.n_intervals = 5;
+    p.n_intervals = intervals;
     p.n_groups = groups;
     p.group_stride = (int32_t)Gs;
     p.n_tracks = (int32_t)tracks;

@@ -35,6 +35,7 @@ MOC_ERR_BAD_INDEX = 7
 MOC_ERR_DEVICE_TIMEOUT = 8
 MOC_ERR_TOO_LARGE = 9
 MOC_ERR_BAD_TRACK = 10
+MOC_ERR_IO = 11
 
 MOC_EXP_FULL = 0
 MOC_EXP_TABLE = 1
@@ -110,6 +111,12 @@ class MocEigenOpts(C.Structure):
                 ("tolerance", C.c_double)]
 
 
+class MocTrackfileInfo(C.Structure):
+    """moc_trackfile_info_t (include/moc_trackfile.h)."""
+    _fields_ = [("n_tracks", C.c_int64), ("n_segments", C.c_int64), ("n_regions", C.c_int32),
+                ("n_intervals", C.c_int32), ("checksum", C.c_uint64)]
+
+
 # moc_track_t as a numpy record (112 bytes)
 TRACK_DTYPE = np.dtype([(n, np.float64) for n in (
     "x0", "y0", "ux", "uy", "rux", "ruy", "ta", "tb", "za", "cot", "rcot", "rsin")] +
@@ -159,6 +166,10 @@ ABI = {
                                   C.POINTER(C.c_int64), _P]),
     "moc_trace_segments": (C.c_int, [_P, C.POINTER(MocGeometry), _P, C.c_int64, _P, _P,
                                      _P, _P, _P]),
+    "moc_trackfile_write": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                      _P, _P, _P, _P]),
+    "moc_trackfile_info": (C.c_int, [C.c_char_p, C.POINTER(MocTrackfileInfo)]),
+    "moc_trackfile_read": (C.c_int, [C.c_char_p, _P, _P, _P, _P]),
     "moc_region_sigT": (C.c_int, [_P, C.POINTER(MocXS), _P, C.c_int32, _P, _P]),
     "moc_source_update": (C.c_int, [_P, C.POINTER(MocXS), _P, C.c_int32, C.c_int32, _P, _P,
                                     C.c_double, _P, _P, _P]),
@@ -513,6 +524,38 @@ def geometry_materials(g) -> np.ndarray:
     R = geometry_regions(g)
     ring = (np.arange(R) // g.n_axial) % (g.n_rings + 1)
     return np.where(ring == g.n_rings, 0, 1 + ring).astype(np.int32)
+
+
+def write_trackfile(path: str, R: int, I: int, off, reg, itv, ds) -> None:
+    """moc_trackfile_write of CSR descriptors (host arrays)."""
+    off = np.ascontiguousarray(off, np.int64)
+    reg = np.ascontiguousarray(reg, np.int32)
+    itv = np.ascontiguousarray(itv, np.uint8)
+    ds = np.ascontiguousarray(ds, np.float32)
+    st = lib().moc_trackfile_write(os.fsencode(path), len(off) - 1, len(reg), R, I,
+                                   off.ctypes.data, reg.ctypes.data, itv.ctypes.data,
+                                   ds.ctypes.data)
+    if st:
+        raise MocError(st)
+
+
+def read_trackfile(path: str):
+    """moc_trackfile_info + moc_trackfile_read: (R, I, offsets, region, interval, ds)."""
+    info = MocTrackfileInfo()
+    L = lib()
+    st = L.moc_trackfile_info(os.fsencode(path), C.byref(info))
+    if st:
+        raise MocError(st)
+    T, S = info.n_tracks, info.n_segments
+    off = np.empty(T + 1, np.int64)
+    reg = np.empty(max(S, 1), np.int32)
+    itv = np.empty(max(S, 1), np.uint8)
+    ds = np.empty(max(S, 1), np.float32)
+    st = L.moc_trackfile_read(os.fsencode(path), off.ctypes.data, reg.ctypes.data,
+                              itv.ctypes.data, ds.ctypes.data)
+    if st:
+        raise MocError(st)
+    return info.n_regions, info.n_intervals, off, reg[:S], itv[:S], ds[:S]
 
 
 def problem_from_tracks(g, off, reg, itv, ds, xs: HostXS):

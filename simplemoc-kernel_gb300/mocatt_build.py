@@ -31,6 +31,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_static.cu", "moc_adjoint.cu",
               "moc_batch.cu", "moc_split.cu", "moc_trace.cu", "moc_transport.cu"]
+HOST_C_SOURCES = ["trackfile.c"]
 # Per-file flags: the track walk rounds every FP64 operation on its own, as the C oracle
 # compiled with -ffp-contract=off does, so its descriptors match the oracle's bit for bit.
 EXTRA_FLAGS = {"moc_trace.cu": ["-fmad=false"], "moc_transport.cu": ["-fmad=false"]}
@@ -85,6 +86,14 @@ def build(verbose: bool = False) -> dict:
         objs.append(o)
         if _stale(o, [s] + hdrs):
             jobs.append([nvcc()] + NVCC_FLAGS + EXTRA_FLAGS.get(src, []) + ["-c", s, "-o", o])
+    # host-only C of the library (the track file format)
+    for src in HOST_C_SOURCES:
+        c = os.path.join(HOST, src)
+        o = os.path.join(BUILD, src.replace(".c", ".o"))
+        objs.append(o)
+        if _stale(o, [c] + hdrs):
+            jobs.append(["gcc", "-std=gnu99", "-O2", "-ffp-contract=off", "-fPIC",
+                         "-I" + INCLUDE, "-c", c, "-o", o])
     synth_src = os.path.join(HOST, "synth.c")
     synth_cmd = None
     if _stale(SYNTH_LIB, [synth_src, os.path.join(INCLUDE, "moc_synth.h")]):

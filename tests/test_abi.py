@@ -28,7 +28,7 @@ def exported(lib_path):
 def test_every_declared_symbol_is_exported():
     syms = exported(os.path.join(mocatt.BUILD, "libmocatt.so"))
     decl = (declared_functions("moc_attenuate.h") + declared_functions("moc_tracks.h") +
-            declared_functions("moc_transport.h"))
+            declared_functions("moc_transport.h") + declared_functions("moc_trackfile.h"))
     assert decl, "no declarations found"
     missing = [n for n in decl if n not in syms]
     assert not missing, missing

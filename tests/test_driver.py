@@ -50,3 +50,27 @@ def test_driver_matches_the_library(handle, table):
         handle.fwd_host(hp, opts)
     ref = float(hp.psi.astype(np.float64).sum())
     assert abs(check - ref) <= 1e-6 * abs(ref), (check, ref)
+
+
+@pytest.mark.gpu
+def test_driver_sweeps_a_track_file(handle):
+    """mocatt_run -f sweeps the golden track file's segments with seeded tables: the same
+    problem through the Python binding gives the same psi sum."""
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                          "tracks_3x2.moctrk")
+    G, n = 8, 1
+    out = run("-f", golden, "-e", str(G), "-n", str(n))
+    assert out.returncode == 0, out.stderr
+    check = float(re.search(r"psi checksum:\s+(\S+)", out.stdout).group(1))
+    R, I, off, reg, itv, ds = mocatt.read_trackfile(golden)
+    T, S = len(off) - 1, len(reg)
+    hp = mocatt.generate(mocatt.Workload("driver", 1, R, I, G, T, S))
+    hp.track_offsets[:] = off
+    hp.seg_region[:] = reg
+    hp.seg_interval[:] = itv
+    hp.seg_ds[:] = ds
+    for _ in range(1 + n):
+        handle.fwd_host(hp, mocatt.default_opts())
+    ref = float(hp.psi.astype(np.float64).sum())
+    assert abs(check - ref) <= 1e-6 * abs(ref), (check, ref)
+
