@@ -203,6 +203,19 @@ struct RevSeg {
 // Full-row gradient reduction of one group, sent only where (unsigned) cell < lim (lim is
 // R*I on active lanes and 0 on idle ones; the null cell R*I sends nothing). Padding groups
 // of an active lane land in the workspace's padding, which the finish pass ignores.
+//
+// Slots of the gradient blocks: within each chunk of 32 VEC groups starting at group b,
+// the q-th group of lane l (group b + VEC l + q) is kept at slot b + L q + l, L the lanes
+// the chunk's storage spans (min(32, (Gs - b) / VEC)). A warp's q-th reduction then covers
+// L consecutive 16-byte slots, whole 32-byte sectors, where slots in group order would
+// leave every sector half-covered by each of two reductions (twice the L2 reduction
+// traffic, which bounds the reverse pass).
+__device__ __forceinline__ int grad_slot(int g, int vec, int Gs)
+{
+    const int b = g / (32 * vec) * (32 * vec), w = g - b;
+    const int L = (Gs - b) / vec < 32 ? (Gs - b) / vec : 32;
+    return b + L * (w % vec) + w / vec;
+}
 __device__ __forceinline__ void red4_if(float4 *p, const float4 &g, int cell, int lim)
 {
     asm volatile("{\n\t.reg .pred q;\n\tsetp.lt.u32 q, %5, %6;\n\t"
@@ -222,7 +235,8 @@ __device__ __forceinline__ void red4_if(float4 *p, const float4 &g, int cell, in
 //   lambda  <- lambda p + W f1.
 template <int VEC>
 __device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg<VEC> &sg,
-                                                Vec<VEC> &lam, float4 *gb, int lim)
+                                                Vec<VEC> &lam, float4 *gb, int gstride,
+                                                int lim)
 {
 #pragma unroll
     for (int q = 0; q < VEC; q++) {
@@ -249,7 +263,7 @@ __device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg
         gs = fmaf(a2, fmaf(la, g3, W * g4), gs);
         gr.x = gs;
         lam.v[q] = fmaf(la, x.p, W * f1);
-        red4_if(gb + sg.c * A.fw.Gs + q, gr, sg.c, lim);
+        red4_if(gb + sg.c * A.fw.Gs + q * gstride, gr, sg.c, lim);
     }
 }
 
@@ -347,7 +361,10 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
         const int gl = act ? g0 : 0;
         const int lim = act ? nullc : 0;
         const float4 *bb = static_cast<const float4 *>(P.blk) + gl;
-        float4 *gb = A.gblk + g0;
+        // this lane's gradient slots: chunk base + lane, then every L slots (grad_slot)
+        const int cb0 = g0 - lane * VEC;
+        const int gstride = (Gs - cb0) / VEC < 32 ? (Gs - cb0) / VEC : 32;
+        float4 *gb = A.gblk + cb0 + lane;
         const bool single = (it.flags & CHUNK_SINGLE) != 0;
         const float *lam_src = single ? A.v + (int64_t)it.t * Gs : A.lam_end + it.q * Gs;
         Vec<VEC> lam;
@@ -378,13 +395,13 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
                 for (int k = 31; k >= klo; k -= 2) {
                     fetch(__shfl_sync(FULL, cA, k - 1), __shfl_sync(FULL, dA, k - 1),
                           wa + k - 1, s1);
-                    reverse_segment<VEC>(A, s0, lam, gb, lim);
+                    reverse_segment<VEC>(A, s0, lam, gb, gstride, lim);
                     const int kn = k - 2;
                     const int cs = kn >= 0 ? cA : cB;
                     const float dsn = kn >= 0 ? dA : dB;
                     fetch(__shfl_sync(FULL, cs, kn & 31), __shfl_sync(FULL, dsn, kn & 31),
                           wa + kn, s0);
-                    reverse_segment<VEC>(A, s1, lam, gb, lim);
+                    reverse_segment<VEC>(A, s1, lam, gb, gstride, lim);
                 }
                 cA = cB;
                 dA = dB;
@@ -569,7 +586,7 @@ struct Jac {
 
 __global__ void adj_finish_kernel(const float4 *__restrict__ gblk, float *__restrict__ d_sigT,
                                   float *__restrict__ d_source, int R, int I, int G, int Gs,
-                                  Jac jac, float mu, float mu2)
+                                  Jac jac, float mu, float mu2, int vec)
 {
     const int64_t n = (int64_t)R * Gs;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
@@ -577,7 +594,7 @@ __global__ void adj_finish_kernel(const float4 *__restrict__ gblk, float *__rest
         const int64_t r = k / Gs;
         const int g = (int)(k - r * Gs);
         if (g >= G) continue;
-        const float4 *cb = gblk + r * I * Gs + g;
+        const float4 *cb = gblk + r * I * Gs + grad_slot(g, vec, Gs);
         float ds = 0.0f;
         for (int i = 0; i < I; i++) ds += cb[(int64_t)i * Gs].x;
         d_sigT[r * Gs + g] = ds;
@@ -674,7 +691,7 @@ cudaError_t launch_adj_starts(const AdjParams &p, cudaStream_t st)
 }
 
 cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,
-                              int G, int Gs, const float *jac27, float mu, float mu2,
+                              int G, int Gs, const float *jac27, float mu, float mu2, int vec,
                               cudaStream_t st)
 {
     Jac j;
@@ -684,7 +701,7 @@ cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     adj_finish_kernel<<<(int)blocks, 256, 0, st>>>(gblk, d_sigT, d_source, R, I, G, Gs, j, mu,
-                                                   mu2);
+                                                   mu2, vec);
     return cudaGetLastError();
 }
 

@@ -1279,7 +1279,8 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     }
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[2], st));
     MOC_CUDA(h, moc::launch_adj_finish(h->gblk, d_sigT, d_source, p->n_regions, p->n_intervals,
-                                       p->n_groups, p->group_stride, jac, o->mu, o->mu2, st));
+                                       p->n_groups, p->group_stride, jac, o->mu, o->mu2, vec,
+                                       st));
     if (prof) {
         MOC_CUDA(h, cudaEventRecord(h->ev[3], st));
         h->timed_launches = launches + 1;

@@ -248,8 +248,9 @@ int adj_map_blocks_per_sm(int vec);
 // dL/dsigT[r][g] = sum over intervals of the sigT gradients; dL/dsource through the
 // transpose of the axial fit (jac[type][k][m]: d q_k / d y_{i+m-1}, type 0 = first
 // interval, 1 = interior, 2 = last), q1 = a1 / mu and q2 = a2 / mu2.
+// vec: the reverse pass's groups per lane, which sets the gradient blocks' slots.
 cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source, int R, int I,
-                              int G, int Gs, const float *jac27, float mu, float mu2,
+                              int G, int Gs, const float *jac27, float mu, float mu2, int vec,
                               cudaStream_t st);
 
 // Track generation (moc_trace.cu). Scratch of a scan over T entries:
