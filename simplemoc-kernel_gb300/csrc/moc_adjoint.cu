@@ -285,55 +285,50 @@ __global__ void __launch_bounds__(256) adj_forward_kernel(const AdjParams A)
         const int nvalid = P.G - g0;
         const bool act = nvalid > 0;
         const int Gs = P.Gs;
-        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        // idle lanes (groups past G) read group 0 and store nothing
+        const float4 *bb = static_cast<const float4 *>(P.blk) + (act ? g0 : 0);
         const float *psi_src = (it.flags & CHUNK_SINGLE) ? P.psi + (int64_t)it.t * Gs
                                                          : P.start + it.q * Gs;
         Vec<VEC> psi;
+#pragma unroll
+        for (int k = 0; k < VEC; k++) psi.v[k] = 0.0f;
         if (act) psi = ld_psi<VEC>(psi_src + g0, nvalid);
-        // descriptor windows A = [wb, wb+32), B = the next 32, as in the forward sweep
+        float *hist = A.hist + g0;
+        // Branch-free, as the forward sweep: descriptor windows A = [wb, wb+32) and B = the
+        // next 32; segments past the end or with bad indices decode to the null cell (an
+        // exact no-op of advance: tau = 0, p = 1, every term 0) and store no history; the
+        // pair loop keeps the blocks of segments k and k+1 in two buffers in turn.
+        const int nullc = P.null_cell;
         int64_t wb = beg;
         int cA, cB;
         float dA, dB;
-        decode(P, wb + lane, beg, end, -1, cA, dA);
-        decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
-        auto desc = [&](int64_t j, int &c, float &d) {
-            int k = (int)(j - wb);
-            if (k >= 32) {
-                cA = cB;
-                dA = dB;
-                wb += 32;
-                k -= 32;
-                decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
+        decode(P, wb + lane, beg, end, nullc, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, nullc, cB, dB);
+        float4 b0[VEC], b1[VEC];
+        int c0 = __shfl_sync(FULL, cA, 0), c1;
+        float d0 = __shfl_sync(FULL, dA, 0), d1;
+        load4<VEC>(bb + c0 * Gs, b0);
+        Vec<VEC> pv, e1v;
+        for (; wb < end; wb += 32) {
+            const int nk = end - wb < 32 ? (int)(end - wb) : 32;
+            for (int k = 0; k < nk; k += 2) {
+                c1 = __shfl_sync(FULL, cA, k + 1);
+                d1 = __shfl_sync(FULL, dA, k + 1);
+                load4<VEC>(bb + c1 * Gs, b1);
+                if (act) st_psi<VEC>(hist + (wb + k) * Gs, psi, nvalid);
+                advance<VEC>(b0, d0, psi, pv, e1v);
+                const int kn = k + 2;
+                const int cs = kn < 32 ? cA : cB;
+                const float dsn = kn < 32 ? dA : dB;
+                c0 = __shfl_sync(FULL, cs, kn & 31);
+                d0 = __shfl_sync(FULL, dsn, kn & 31);
+                load4<VEC>(bb + c0 * Gs, b0);
+                if (act && k + 1 < nk) st_psi<VEC>(hist + (wb + k + 1) * Gs, psi, nvalid);
+                advance<VEC>(b1, d1, psi, pv, e1v);
             }
-            c = __shfl_sync(FULL, cA, k);
-            d = __shfl_sync(FULL, dA, k);
-        };
-        int c0 = -1;
-        float d0 = 0.0f;
-        float4 b0[VEC];
-        if (beg < end) {
-            desc(beg, c0, d0);
-            if (c0 >= 0 && act) load4<VEC>(bb + c0 * Gs, b0);
-        }
-        for (int64_t j = beg; j < end; j++) {
-            int c1 = -1;
-            float d1 = 0.0f;
-            float4 b1[VEC];
-            if (j + 1 < end) {
-                desc(j + 1, c1, d1);
-                if (c1 >= 0 && act) load4<VEC>(bb + c1 * Gs, b1);
-            }
-            if (act) {
-                st_psi<VEC>(A.hist + j * Gs + g0, psi, nvalid);
-                if (c0 >= 0) {
-                    Vec<VEC> pv, e1v;
-                    advance<VEC>(b0, d0, psi, pv, e1v);
-                }
-            }
-            c0 = c1;
-            d0 = d1;
-#pragma unroll
-            for (int v = 0; v < VEC; v++) b0[v] = b1[v];
+            cA = cB;
+            dA = dB;
+            decode(P, wb + 64 + lane, beg, end, nullc, cB, dB);
         }
     }
 }
