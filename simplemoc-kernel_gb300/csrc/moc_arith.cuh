@@ -85,11 +85,11 @@ __device__ __forceinline__ void attenuate_pair(const float4 &x0, const float4 &x
     const float2 tt = __fmul2_rn(tau, tau);
     float2 e, p, tme, cub3;
     if constexpr (EK == EXPK_STABLE) {
-        const ExpTerms u = exp_terms_stable(tau.x), w = exp_terms_stable(tau.y);
-        e = make_float2(u.e, w.e);
-        p = make_float2(u.p, w.p);
-        tme = make_float2(u.tme, w.tme);
-        cub3 = __fmul2_rn(make_float2(u.cub, w.cub), make_float2(1.0f / 3.0f, 1.0f / 3.0f));
+        const ExpTerms2 u = exp_terms_stable2(tau);
+        e = u.e;
+        p = u.p;
+        tme = u.tme;
+        cub3 = __fmul2_rn(u.cub, make_float2(1.0f / 3.0f, 1.0f / 3.0f));
     } else {
         if constexpr (EK == EXPK_TABLE) {
             e = make_float2(table_lookup(tr.tab, tr.n, tr.dx, tr.max, tau.x),

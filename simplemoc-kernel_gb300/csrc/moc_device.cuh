@@ -243,7 +243,8 @@ __device__ __forceinline__ float exp_neg_rr(float tau)
     const float L2E_LO = 1.9259629911266175e-8f;         // log2(e) - L2E_HI
     const float LN2 = 0.693147180559945309f;
     const float hi = -tau * L2E_HI;
-    const float lo = fmaf(-tau, L2E_HI, -hi) - tau * L2E_LO;
+    // the rounding error of hi, then the tail of log2(e), each in one fused step
+    const float lo = fmaf(-tau, L2E_LO, fmaf(-tau, L2E_HI, -hi));
     const float p = ex2_approx(hi);
     return fmaf(p, lo * LN2, p);
 }
@@ -290,6 +291,62 @@ __device__ __forceinline__ ExpTerms exp_terms_stable(float tau)
         r.e = 1.0f - r.p;
         r.tme = tau - r.e;
         r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
+    }
+    return r;
+}
+
+// exp_terms_stable for two groups at once on the packed FP32 pipe: every packed operation
+// stands for the scalar one above in the same order (a - b and 1 - x as fma(b, -1, a) and
+// fma(x, -1, 1), which round once to the same value), so the terms are the scalar ones bit
+// for bit. A pair straddling tau = 2 takes the scalar form per group.
+struct ExpTerms2 {
+    float2 e, p, tme, cub;
+};
+
+__device__ __forceinline__ ExpTerms2 exp_terms_stable2(float2 tau)
+{
+    ExpTerms2 r;
+    const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
+    const float2 mt = make_float2(-tau.x, -tau.y);
+    auto c = [](float v) { return make_float2(v, v); };
+    if (tau.x < 2.0f && tau.y < 2.0f) {
+        float2 h = c(1.0f / 20922789888000.0f);
+        h = __ffma2_rn(h, mt, c(1.0f / 1307674368000.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 87178291200.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 6227020800.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 479001600.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 39916800.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 3628800.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 362880.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 40320.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 5040.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 720.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 120.0f));
+        h = __ffma2_rn(h, mt, c(1.0f / 24.0f));
+        const float2 t2 = __fmul2_rn(tau, tau);
+        const float2 s4 = __fmul2_rn(__fmul2_rn(h, t2), t2);
+        r.cub = __fmul2_rn(c(6.0f), s4);
+        r.tme = __ffma2_rn(t2, __ffma2_rn(tau, c(-1.0f / 6.0f), c(0.5f)), s4);
+        r.e = __ffma2_rn(r.tme, mone, tau);
+        r.p = __ffma2_rn(r.e, mone, one);
+    } else if (tau.x >= 2.0f && tau.y >= 2.0f) {
+        const float L2E_HI = 1.44269502162933349609375f, L2E_LO = 1.9259629911266175e-8f;
+        const float LN2 = 0.693147180559945309f;
+        const float2 hi = __fmul2_rn(mt, c(L2E_HI));
+        const float2 lo = __ffma2_rn(mt, c(L2E_LO),
+                                     __ffma2_rn(mt, c(L2E_HI), make_float2(-hi.x, -hi.y)));
+        const float2 q = make_float2(ex2_approx(hi.x), ex2_approx(hi.y));
+        r.p = __ffma2_rn(q, __fmul2_rn(lo, c(LN2)), q);
+        r.e = __ffma2_rn(r.p, mone, one);
+        r.tme = __ffma2_rn(r.e, mone, tau);
+        r.cub = __ffma2_rn(__fmul2_rn(tau, tau), __fadd2_rn(tau, c(-3.0f)),
+                           __fmul2_rn(c(6.0f), r.tme));
+    } else {
+        const ExpTerms u = exp_terms_stable(tau.x), w = exp_terms_stable(tau.y);
+        r.e = make_float2(u.e, w.e);
+        r.p = make_float2(u.p, w.p);
+        r.tme = make_float2(u.tme, w.tme);
+        r.cub = make_float2(u.cub, w.cub);
     }
     return r;
 }
