@@ -37,6 +37,15 @@ __device__ __forceinline__ Vec<VEC> ld_row(const float *p)
     return r;
 }
 
+// Two consecutive float4 (32 bytes, 32-byte aligned) in one 256-bit read-only load.
+__device__ __forceinline__ void ldg_2x4(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z),
+          "=f"(b.w)
+        : "l"(p));
+}
+
 // Plain (coherent) row load/store for psi, which the sweep owns.
 template <int VEC>
 __device__ __forceinline__ Vec<VEC> ld_psi(const float *p, int n_valid)

@@ -162,8 +162,15 @@ __device__ __forceinline__ void load_blk(const void *base, int idx, Blk<VEC> &b)
 {
     if constexpr (ST == STORE_F32) {
         const float4 *p = static_cast<const float4 *>(base) + idx;
+        if constexpr (VEC % 2 == 0) {
+            // idx is even (a lane's first group) and rows are multiples of 4 groups, so
+            // each pair of blocks is 32-byte aligned: one 256-bit load per pair
 #pragma unroll
-        for (int k = 0; k < VEC; k++) b.v[k] = __ldg(p + k);
+            for (int k = 0; k < VEC; k += 2) ldg_2x4(p + k, b.v[k], b.v[k + 1]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < VEC; k++) b.v[k] = __ldg(p + k);
+        }
     } else {
         const uint2 *p = static_cast<const uint2 *>(base) + idx;
         uint2 w[VEC];
