@@ -5,6 +5,8 @@
 2. Where the reference sources are present, the pin is re-run live on fresh seeds.
 3. The FP64 oracle and its error-magnitude companion bound the FP32 restatement.
 4. The FP64 adjoint agrees with FP64 central differences.
+5. What the 16-bit storage of the precision forms does to the problem itself (the storage
+   term, reported apart from the forms' arithmetic error).
 """
 import os
 import platform
@@ -130,6 +132,36 @@ def test_fp64_series_branch_continuity():
         q.seg_ds[:] = ds
         outs.append(oracle.fwd_fp64(q)["psi"][0, :4])
     np.testing.assert_allclose(outs[0], outs[1], rtol=1e-6)
+
+
+@pytest.mark.parametrize("prec,u", [(mocatt.MOC_PREC_BF16, 2.0 ** -9),
+                                     (mocatt.MOC_PREC_FP16, 2.0 ** -11)])
+def test_storage_rounding_effect(prec, u):
+    """What 16-bit storage does to the problem itself, apart from any arithmetic: the FP64
+    oracle on the cell blocks as a 16-bit form stores them (sigT and the FP32 axial
+    coefficients rounded to nearest) against the FP64 oracle on the FP32 inputs, on the
+    wide-tau inputs the forms are graded on. The forms' own arithmetic error is measured
+    against the first of these (on the GPU); this is the separate storage term. Normwise,
+    the outputs move by about the storage format's unit roundoff u, between u / 8 and 4 u:
+    BF16 storage shifts psi and fine_flux by ~4e-3, FP16 by ~5e-4, far above 1e-5."""
+    hp = mocatt.generate(mocatt.WORKLOADS["widetau_50M_g128"].with_(
+        regions=400, tracks=400, segments=200_000))
+    ref = oracle.fwd_fp64(hp)
+    qp, coef = oracle.quantized_inputs(hp, prec)
+    q = oracle.fwd_fp64_coef(qp, coef)
+    G = hp.G
+    out = {}
+    for k in ("psi", "ff"):
+        d = q[k][:, :G] - ref[k][:, :G]
+        out[k] = float(np.linalg.norm(d) / np.linalg.norm(ref[k][:, :G]))
+        assert u / 8 <= out[k] <= 4 * u, (k, out[k], u)
+    print("storage rounding, normwise:", out)
+    # the FP32 fit of the coefficients alone (what FP32 storage stores) is ~1e-7
+    qp, coef = oracle.quantized_inputs(hp, mocatt.MOC_PREC_FP32_STABLE)
+    q = oracle.fwd_fp64_coef(qp, coef)
+    for k in ("psi", "ff"):
+        d = q[k][:, :G] - ref[k][:, :G]
+        assert np.linalg.norm(d) / np.linalg.norm(ref[k][:, :G]) <= 1e-6
 
 
 def test_fp32_omp_matches_sequential():
