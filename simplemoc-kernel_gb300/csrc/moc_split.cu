@@ -201,13 +201,6 @@ __global__ void split_start_kernel(const SweepParams P, const SplitWork W)
     }
 }
 
-int grid_for(int64_t n)
-{
-    int64_t b = (n + 255) / 256;
-    if (b > 152 * 16) b = 152 * 16;
-    return (int)(b < 1 ? 1 : b);
-}
-
 }  // namespace
 
 int64_t split_max_records(int64_t T, int64_t S, int chunk)

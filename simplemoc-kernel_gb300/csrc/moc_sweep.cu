@@ -542,14 +542,14 @@ __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
         for (int64_t item = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
              item < n_items; item += nw)
             sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, n_units, lane, tr, ring);
-        return;
-    }
-    for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(P.counter, 1ULL);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= (unsigned long long)n_items) break;
-        sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, n_units, lane, tr, ring);
+    } else {
+        for (;;) {
+            unsigned long long item = 0;
+            if (lane == 0) item = atomicAdd(P.counter, 1ULL);
+            item = __shfl_sync(FULL, item, 0);
+            if (item >= (unsigned long long)n_items) break;
+            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, n_units, lane, tr, ring);
+        }
     }
 }
 
