@@ -45,7 +45,7 @@
 extern "C" {
 #endif
 
-#define MOC_ABI_VERSION 3
+#define MOC_ABI_VERSION 4
 
 typedef enum {
     MOC_OK = 0,
@@ -141,10 +141,12 @@ typedef struct {
                                      batching form: 1..8)                                 */
     int32_t profile;              /* 1: time each kernel of the call with CUDA events on
                                      the call's stream (read with moc_last_timings)      */
-    int32_t prefetch;             /* segments whose cell blocks are in flight ahead of the
-                                     arithmetic: 0 = auto, 1 = one (registers), 8 = seven,
-                                     through a cp.async ring in shared memory (plain and
-                                     stable FP32 forms with FP32 tallies)                  */
+    int32_t prefetch;             /* how far ahead of the arithmetic segments' cell blocks
+                                     are fetched: 0 = auto, 1 = one segment, in registers;
+                                     2..16 = a ring of that many slots per warp in shared
+                                     memory, filled by bulk copies (the TMA engine), so
+                                     prefetch - 1 segments are in flight (FP32 storage with
+                                     FP32 tallies: MOC_PREC_FP32, MOC_PREC_FP32_STABLE)  */
     int32_t track_chunk;          /* long tracks sweep in parallel chunks: a track of more
                                      than 4 * C segments is cut into chunks of C segments,
                                      joined through the affine form of the psi recursion.
@@ -280,11 +282,22 @@ moc_status_t moc_attenuate_adj(moc_handle_t handle, const moc_problem_t *problem
  * MOC_ERR_TOO_LARGE.
  *
  * The first call on each device looks up the array's device address (once, with that
- * device current); make that first call before any stream capture. Every call shares
- * the one array, and it keeps the last call's contents: calls whose kernels overlap on
- * the GPU race on it, so order them on one stream. Out-of-range segment indices are
- * skipped by the kernel; with opts->checked = 1 the call validates first, waits, and
- * returns MOC_ERR_BAD_INDEX without touching psi or fine_flux.
+ * device current); make that first call before any stream capture. The address is kept
+ * for the life of the process: after cudaDeviceReset of a device (which unloads the
+ * library's device image there) this entry point must not be called on that device
+ * again. Every call shares the one array, and it keeps the last call's contents: calls
+ * whose kernels overlap on the GPU race on it, so order them on one stream. Every array
+ * of `problem` must be memory of the current device (or managed memory), else
+ * MOC_ERR_INVALID_ARG.
+ *
+ * Bad input: with opts->checked = 1 the call validates every offset and index first,
+ * waits for that check on `stream` (cudaStreamSynchronize), and returns
+ * MOC_ERR_BAD_INDEX without touching psi or fine_flux. With opts->checked = 0 the
+ * kernels skip out-of-range segments and tracks whose offsets leave [0, S] without
+ * reporting them: this entry point has no handle whose error word a later call could
+ * read, so callers that need the report pass checked = 1. In table mode the table is
+ * built in a static host buffer and copied from it on `stream`; the next call rewrites
+ * that buffer.
  */
 #define MOC_NOALLOC_MAX_CELL_GROUPS 655360 /* 10 MiB of cell blocks */
 #define MOC_NOALLOC_MAX_TABLE_POINTS 24000
@@ -298,7 +311,9 @@ moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *problem,
  * segment or track is skipped by the sweep (nothing is read or written through its
  * indices); the rest of the sweep completes. MOC_ERR_BAD_TRACK (first) if a
  * moc_trace_segments call since then met an invalid track record or one whose segment
- * count disagreed with the offsets (include/moc_tracks.h).
+ * count disagreed with the offsets (include/moc_tracks.h). MOC_ERR_DEVICE_TIMEOUT (next)
+ * if a sweep with a bulk-copy ring (opts.prefetch > 1) gave up waiting for a copy (each
+ * warp waits about a second at most): its results are incomplete.
  */
 moc_status_t moc_synchronize(moc_handle_t handle, void *stream);
 

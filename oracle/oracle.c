@@ -92,73 +92,106 @@ static int table_make(const moc_fwd_opts_t *o, table_t *t)
 }
 
 /* ------------------------------------------------------------------------------------
- * FP32 restatement of attenuate_segment, src/cpu/kernel.c:99-332, one group at a time.
+ * FP32 restatement of attenuate_segment, src/cpu/kernel.c:99-332.
  * Every expression keeps the reference's operand order and grouping (C evaluates
  * a*b*c as (a*b)*c), so the rounding is the same; ds is the segment's own length
- * where the reference hard-codes 0.7f (kernel.c:104).
+ * where the reference hard-codes 0.7f (kernel.c:104). The work is split into the same
+ * per-group passes over scratch vectors as the reference's (one pass per quantity), so
+ * that a build with the reference's optimisation flags vectorises it the way it
+ * vectorises the reference; per element the operations are unchanged.
  * ---------------------------------------------------------------------------------- */
+typedef struct {
+    float *q0, *q1, *q2, *sig, *tau, *sig2, *ev, *reuse, *fi, *tally, *t1, *t2, *t3, *t4;
+    float *mem;
+} vecs_t;
+
+static int vecs_make(vecs_t *v, int64_t n)
+{
+    v->mem = (float *)malloc((size_t)(14 * n) * sizeof(float));
+    if (!v->mem) return -1;
+    float **f[] = {&v->q0, &v->q1, &v->q2, &v->sig, &v->tau, &v->sig2, &v->ev, &v->reuse,
+                   &v->fi, &v->tally, &v->t1, &v->t2, &v->t3, &v->t4};
+    for (int k = 0; k < 14; k++) *f[k] = v->mem + k * n;
+    return 0;
+}
+
+/* Fills v->tally (weight * flux integral per group) and updates state_flux. */
 static void attenuate_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o,
                            const table_t *tab, int32_t region, int32_t fai, float ds,
-                           float *state_flux, float *fsr_flux)
+                           float *restrict state_flux, const vecs_t *v)
 {
     const float dz = o->dz, zin = o->zin, weight = o->weight, mu = o->mu, mu2 = o->mu2;
     const int64_t Gs = p->group_stride;
     const int G = p->n_groups, I = p->n_intervals;
-    const float *src = p->source + (int64_t)region * I * Gs;
-    const float *sig = p->sigT + (int64_t)region * Gs;
+    const float *restrict src = p->source + (int64_t)region * I * Gs;
+    const float *restrict sg = p->sigT + (int64_t)region * Gs;
+    float *restrict q0 = v->q0, *restrict q1 = v->q1, *restrict q2 = v->q2;
+    float *restrict sigT = v->sig, *restrict tau = v->tau, *restrict sigT2 = v->sig2;
+    float *restrict expVal = v->ev, *restrict reuse = v->reuse, *restrict fi = v->fi;
+    float *restrict tally = v->tally, *restrict t1 = v->t1, *restrict t2 = v->t2;
+    float *restrict t3 = v->t3, *restrict t4 = v->t4;
 
-    for (int g = 0; g < G; g++) {
-        float q0, q1, q2;
-        if (fai == 0) {                                      /* kernel.c:111-133 */
-            const float y2 = src[(int64_t)fai * Gs + g];
-            const float y3 = src[(int64_t)(fai + 1) * Gs + g];
+    if (fai == 0) {                                          /* kernel.c:111-133 */
+        const float *restrict f2 = src + (int64_t)fai * Gs;
+        const float *restrict f3 = src + (int64_t)(fai + 1) * Gs;
+        for (int g = 0; g < G; g++) {
+            const float y2 = f2[g], y3 = f3[g];
             const float c0 = y2;
             const float c1 = (y3 - y2) / dz;
-            q0 = c0 + c1 * zin;
-            q1 = c1;
-            q2 = 0;
-        } else if (fai == I - 1) {                           /* kernel.c:134-156 */
-            const float y1 = src[(int64_t)(fai - 1) * Gs + g];
-            const float y2 = src[(int64_t)fai * Gs + g];
+            q0[g] = c0 + c1 * zin;
+            q1[g] = c1;
+            q2[g] = 0;
+        }
+    } else if (fai == I - 1) {                               /* kernel.c:134-156 */
+        const float *restrict f1 = src + (int64_t)(fai - 1) * Gs;
+        const float *restrict f2 = src + (int64_t)fai * Gs;
+        for (int g = 0; g < G; g++) {
+            const float y1 = f1[g], y2 = f2[g];
             const float c0 = y2;
             const float c1 = (y2 - y1) / dz;
-            q0 = c0 + c1 * zin;
-            q1 = c1;
-            q2 = 0;
-        } else {                                             /* kernel.c:157-191 */
-            const float y1 = src[(int64_t)(fai - 1) * Gs + g];
-            const float y2 = src[(int64_t)fai * Gs + g];
-            const float y3 = src[(int64_t)(fai + 1) * Gs + g];
+            q0[g] = c0 + c1 * zin;
+            q1[g] = c1;
+            q2[g] = 0;
+        }
+    } else {                                                 /* kernel.c:157-191 */
+        const float *restrict f1 = src + (int64_t)(fai - 1) * Gs;
+        const float *restrict f2 = src + (int64_t)fai * Gs;
+        const float *restrict f3 = src + (int64_t)(fai + 1) * Gs;
+        for (int g = 0; g < G; g++) {
+            const float y1 = f1[g], y2 = f2[g], y3 = f3[g];
             const float c0 = y2;
             const float c1 = (y1 - y3) / (2.f * dz);
             const float c2 = (y1 - 2.f * y2 + y3) / (2.f * dz * dz);
-            q0 = c0 + c1 * zin + c2 * zin * zin;
-            q1 = c1 + 2.f * c2 * zin;
-            q2 = c2;
+            q0[g] = c0 + c1 * zin + c2 * zin * zin;
+            q1[g] = c1 + 2.f * c2 * zin;
+            q2[g] = c2;
         }
-        const float sigT = sig[g];                           /* kernel.c:200-208 */
-        const float tau = sigT * ds;
-        const float sigT2 = sigT * sigT;
-        float expVal;                                        /* kernel.c:216-223 */
-        if (tab->values)
-            expVal = oracle_table_lookup(tab->values, tab->dx, tab->lookup_max, tau);
-        else
-            expVal = 1.f - expf(-tau);
-        /* kernel.c:233-237: only the last term is divided (C precedence) */
-        const float reuse = tau * (tau - 2.f) + 2.f * expVal / (sigT * sigT2);
-        /* kernel.c:245-252 */
-        const float flux_integral = (q0 * tau + (sigT * state_flux[g] - q0) * expVal) / sigT2 +
-                                    q1 * mu * reuse +
-                                    q2 * mu2 * (tau * (tau * (tau - 3.f) + 6.f) - 6.f * expVal) /
-                                        (3.f * sigT2 * sigT2);
-        const float tally = weight * flux_integral;          /* kernel.c:259-263 */
-        fsr_flux[g] += tally;                                /* kernel.c:275-278 */
-        const float t1 = q0 * expVal / sigT;                 /* kernel.c:289-331 */
-        const float t2 = q1 * mu * (tau - expVal) / sigT2;
-        const float t3 = q2 * mu2 * reuse;
-        const float t4 = state_flux[g] * (1.f - expVal);
-        state_flux[g] = t1 + t2 + t3 + t4;
     }
+    for (int g = 0; g < G; g++) {                            /* kernel.c:200-208 */
+        sigT[g] = sg[g];
+        tau[g] = sigT[g] * ds;
+        sigT2[g] = sigT[g] * sigT[g];
+    }
+    if (tab->values) {                                       /* kernel.c:216-223 */
+        for (int g = 0; g < G; g++)
+            expVal[g] = oracle_table_lookup(tab->values, tab->dx, tab->lookup_max, tau[g]);
+    } else {
+        for (int g = 0; g < G; g++) expVal[g] = 1.f - expf(-tau[g]);
+    }
+    /* kernel.c:233-237: only the last term is divided (C precedence) */
+    for (int g = 0; g < G; g++)
+        reuse[g] = tau[g] * (tau[g] - 2.f) + 2.f * expVal[g] / (sigT[g] * sigT2[g]);
+    for (int g = 0; g < G; g++)                              /* kernel.c:245-252 */
+        fi[g] = (q0[g] * tau[g] + (sigT[g] * state_flux[g] - q0[g]) * expVal[g]) / sigT2[g] +
+                q1[g] * mu * reuse[g] +
+                q2[g] * mu2 * (tau[g] * (tau[g] * (tau[g] - 3.f) + 6.f) - 6.f * expVal[g]) /
+                    (3.f * sigT2[g] * sigT2[g]);
+    for (int g = 0; g < G; g++) tally[g] = weight * fi[g];  /* kernel.c:259-263 */
+    for (int g = 0; g < G; g++) t1[g] = q0[g] * expVal[g] / sigT[g];  /* kernel.c:289-331 */
+    for (int g = 0; g < G; g++) t2[g] = q1[g] * mu * (tau[g] - expVal[g]) / sigT2[g];
+    for (int g = 0; g < G; g++) t3[g] = q2[g] * mu2 * reuse[g];
+    for (int g = 0; g < G; g++) t4[g] = state_flux[g] * (1.f - expVal[g]);
+    for (int g = 0; g < G; g++) state_flux[g] = t1[g] + t2[g] + t3[g] + t4[g];
 }
 
 int oracle_fwd_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o)
@@ -166,6 +199,11 @@ int oracle_fwd_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o)
     if (!problem_ok(p, o)) return -1;
     table_t tab;
     if (table_make(o, &tab)) return -1;
+    vecs_t v;
+    if (vecs_make(&v, p->group_stride)) {
+        free(tab.values);
+        return -1;
+    }
     const int64_t Gs = p->group_stride;
     for (int32_t t = 0; t < p->n_tracks; t++) {
         float *psi = p->psi + (int64_t)t * Gs;
@@ -173,9 +211,11 @@ int oracle_fwd_fp32(const moc_problem_t *p, const moc_fwd_opts_t *o)
             const int32_t r = p->seg_region[j];
             const int32_t i = p->seg_interval[j];
             float *ff = p->fine_flux + ((int64_t)r * p->n_intervals + i) * Gs;
-            attenuate_fp32(p, o, &tab, r, i, p->seg_ds[j], psi, ff);
+            attenuate_fp32(p, o, &tab, r, i, p->seg_ds[j], psi, &v);
+            for (int g = 0; g < p->n_groups; g++) ff[g] += v.tally[g];  /* kernel.c:275-278 */
         }
     }
+    free(v.mem);
     free(tab.values);
     return 0;
 }
@@ -198,33 +238,36 @@ int oracle_fwd_fp32_omp(const moc_problem_t *p, const moc_fwd_opts_t *o, int nth
     }
     for (int64_t c = 0; c < ncell; c++) omp_init_lock(&locks[c]);
     if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel num_threads(nthreads)
+    int failed = 0;
+#pragma omp parallel num_threads(nthreads) reduction(| : failed)
     {
-        float *scratch = (float *)malloc((size_t)Gs * 2 * sizeof(float));
-        float *tally = scratch + Gs;
+        vecs_t v;
+        if (vecs_make(&v, Gs)) {
+            failed = 1;
+        } else {
 #pragma omp for schedule(dynamic, 16)
-        for (int32_t t = 0; t < p->n_tracks; t++) {
-            float *psi = p->psi + (int64_t)t * Gs;
-            for (int64_t j = p->track_offsets[t]; j < p->track_offsets[t + 1]; j++) {
-                const int32_t r = p->seg_region[j];
-                const int32_t i = p->seg_interval[j];
-                const int64_t c = (int64_t)r * p->n_intervals + i;
-                /* The tally is formed into a private row and added under the cell's
-                 * lock, as kernel.c:265-281 does. */
-                memset(tally, 0, (size_t)p->n_groups * sizeof(float));
-                attenuate_fp32(p, o, &tab, r, i, p->seg_ds[j], psi, tally);
-                float *ff = p->fine_flux + c * Gs;
-                omp_set_lock(&locks[c]);
-                for (int g = 0; g < p->n_groups; g++) ff[g] += tally[g];
-                omp_unset_lock(&locks[c]);
+            for (int32_t t = 0; t < p->n_tracks; t++) {
+                float *psi = p->psi + (int64_t)t * Gs;
+                for (int64_t j = p->track_offsets[t]; j < p->track_offsets[t + 1]; j++) {
+                    const int32_t r = p->seg_region[j];
+                    const int32_t i = p->seg_interval[j];
+                    const int64_t c = (int64_t)r * p->n_intervals + i;
+                    /* The tally is formed into a private row and added under the cell's
+                     * lock, as kernel.c:265-281 does. */
+                    attenuate_fp32(p, o, &tab, r, i, p->seg_ds[j], psi, &v);
+                    float *ff = p->fine_flux + c * Gs;
+                    omp_set_lock(&locks[c]);
+                    for (int g = 0; g < p->n_groups; g++) ff[g] += v.tally[g];
+                    omp_unset_lock(&locks[c]);
+                }
             }
+            free(v.mem);
         }
-        free(scratch);
     }
     for (int64_t c = 0; c < ncell; c++) omp_destroy_lock(&locks[c]);
     free(locks);
     free(tab.values);
-    return 0;
+    return failed ? -1 : 0;
 #endif
 }
 

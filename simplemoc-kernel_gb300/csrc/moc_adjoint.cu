@@ -679,7 +679,7 @@ cudaError_t launch_adj_starts(const AdjParams &p, cudaStream_t st)
 {
     const int64_t warps = (int64_t)p.fw.T * ((p.fw.G + 31) / 32) * 2;
     int64_t blocks = (warps * 32 + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > grid_cap(16)) blocks = grid_cap(16);
     if (blocks < 1) blocks = 1;
     adj_start_kernel<<<(int)blocks, 256, 0, st>>>(p);
     return cudaGetLastError();
@@ -694,7 +694,7 @@ cudaError_t launch_adj_finish(const float4 *gblk, float *d_sigT, float *d_source
     const int64_t n = (int64_t)R * Gs;
     if (n == 0) return cudaSuccess;
     int64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > grid_cap(16)) blocks = grid_cap(16);
     adj_finish_kernel<<<(int)blocks, 256, 0, st>>>(gblk, d_sigT, d_source, R, I, G, Gs, j, mu,
                                                    mu2, vec);
     return cudaGetLastError();

@@ -147,12 +147,12 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         return MOC_ERR_INVALID_ARG;
     if (o->vec != 0 && o->vec != 1 && o->vec != 2 && o->vec != 4) return MOC_ERR_INVALID_ARG;
     if (o->warps_per_block < 0 || o->warps_per_block > 16) return MOC_ERR_INVALID_ARG;
-    if (o->prefetch != 0 && o->prefetch != 1 && o->prefetch != moc::RING_DEPTH)
-        return MOC_ERR_INVALID_ARG;
+    if (o->prefetch < 0 || o->prefetch > moc::RING_MAX) return MOC_ERR_INVALID_ARG;
     if (o->track_chunk != 0 && o->track_chunk != -1 &&
         (o->track_chunk < 32 || o->track_chunk > moc::SPLIT_CHUNK_MAX))
         return MOC_ERR_INVALID_ARG;
-    if (o->prefetch == moc::RING_DEPTH &&
+    // the bulk-copy ring: FP32 cell blocks and FP32 tallies
+    if (o->prefetch > 1 &&
         (o->precision == MOC_PREC_BF16 || o->precision == MOC_PREC_FP16 ||
          o->tally != MOC_TALLY_ATOMIC_FP32))
         return MOC_ERR_UNSUPPORTED;
@@ -165,8 +165,9 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
     return MOC_OK;
 }
 
-// Device pointers must be device or managed memory.
-bool device_accessible(const void *p)
+// Device pointers must be memory of device `dev` or managed memory: a sweep on one device
+// does not read or write another device's memory (it may have no peer access to it).
+bool device_accessible(const void *p, int dev)
 {
     if (!p) return true;
     cudaPointerAttributes a;
@@ -174,7 +175,8 @@ bool device_accessible(const void *p)
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 moc_status_t ensure(moc_handle_t h, void **buf, size_t *cap, size_t bytes)
@@ -229,8 +231,9 @@ int auto_chunk_steps(double warp_steps)
 int auto_chunk(int64_t S, int64_t n_gch) { return auto_chunk_steps((double)S * (double)n_gch); }
 
 // Whether long tracks are split (opts.track_chunk, and S long enough for any track to be
-// cut), and if so the split workspace, wired into *sp. Record and map counts share one
-// 64-bit scan, so both must stay below 2^31. n_gch: group chunks per track.
+// cut), and if so the split workspace, wired into *sp. The workspace holds at most
+// split_max_records records (below 2^31, record ids are stored in 32-bit fields); offsets
+// that ask for more have the excess dropped and reported. n_gch: group chunks per track.
 moc_status_t split_setup(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
                          int map_all, int64_t n_gch, moc::SweepParams *sp, moc::SplitWork *sw,
                          bool *split)
@@ -248,7 +251,7 @@ moc_status_t split_setup(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
     if ((s = ensure(h, reinterpret_cast<void **>(&h->sbase), &h->sbase_cap,
                     (size_t)(T + 1) * sizeof(int64_t))) ||
         (s = ensure(h, reinterpret_cast<void **>(&h->sbsum), &h->sbsum_cap,
-                    (size_t)nb * sizeof(int64_t))) ||
+                    2 * (size_t)nb * sizeof(int64_t))) ||
         (s = ensure(h, reinterpret_cast<void **>(&h->srec), &h->srec_cap,
                     (size_t)cap * sizeof(int4))) ||
         (s = ensure(h, reinterpret_cast<void **>(&h->smlist), &h->smlist_cap,
@@ -299,6 +302,9 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
                                                      : moc::TALLY_F32;
     }
     c->prefetch = o->prefetch > 1 ? o->prefetch : 1;
+    // the bulk-copy ring reads the lane-strided layout of the pair layout (or of one
+    // group per lane)
+    if (moc::fwd_bulk(*c) && vec > 1 && !moc::f32_pairs(vec)) return MOC_ERR_UNSUPPORTED;
     // the branch-free segment loop needs whole rows per lane (and the null-cell row,
     // which fwd_device writes after the cell blocks)
     c->branch_free = p->n_groups % vec == 0;
@@ -381,10 +387,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if ((s = split_setup(h, p, o, 0, sp.n_chunks, &sp, &sw, &split))) return s;
     moc::FwdConfig mcfg = cfg;
     if (split) {
-        mcfg.mode = 1;
-        mcfg.prefetch = (cfg.prefetch == moc::RING_DEPTH && cfg.store == moc::STORE_F32)
-                            ? moc::RING_DEPTH
-                            : 1;
+        mcfg.mode = 1;  // the same loop and block layout as the sweep
         mcfg.tally = moc::TALLY_F32;
         const int per_sm = moc::fwd_blocks_per_sm(mcfg, o->table_points);
         if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
@@ -398,7 +401,8 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     if (prep && cfg.store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
-                                           o->mu, o->mu2, st, true, moc::f32_pairs(cfg.vec)));
+                                           o->mu, o->mu2, st, true, moc::f32_pairs(cfg.vec),
+                                           moc::fwd_bulk(cfg) ? cfg.vec : 0));
     else if (prep)
         MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
                                              p->n_regions, p->n_intervals, p->group_stride,
@@ -413,7 +417,7 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
         moc::SweepParams mp = sp;
         mp.counter = ctr + 1;
         MOC_CUDA(h, moc::launch_fwd(mp, mcfg, st));
-        MOC_CUDA(h, moc::launch_split_start(sp, sw, st));
+        MOC_CUDA(h, moc::launch_split_start(sp, sw, h->sm_count, st));
     }
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[4], st));
     MOC_CUDA(h, moc::launch_fwd(sp, cfg, st));
@@ -440,7 +444,7 @@ moc_status_t check_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
     for (int32_t k = 0; k < n; k++) {
         moc_status_t s = check_problem(&probs[k], o);
         if (s) return s;
-        if (!moc::all_device_accessible(&probs[k])) return MOC_ERR_INVALID_ARG;
+        if (!moc::all_device_accessible(&probs[k], h->device)) return MOC_ERR_INVALID_ARG;
     }
     return MOC_OK;
 }
@@ -511,7 +515,7 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
         perm_total += X.on[k] ? (size_t)cap[k] : (size_t)p.n_tracks;
         if (X.on[k]) {
             const size_t T = p.n_tracks, Gs = p.group_stride, c = cap[k];
-            split_bytes += align_up((T + 1) * 8) + align_up((T + 1023) / 1024 * 8) +
+            split_bytes += align_up((T + 1) * 8) + align_up((T + 1023) / 1024 * 16) +
                            align_up(c * 16) + align_up((c + 1) * 8) + 3 * align_up(c * Gs * 4);
         }
     }
@@ -565,7 +569,7 @@ moc_status_t build_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,
             sw.base = reinterpret_cast<int64_t *>(base);
             base += align_up((T + 1) * 8);
             sw.bsum = reinterpret_cast<int64_t *>(base);
-            base += align_up((T + 1023) / 1024 * 8);
+            base += align_up((T + 1023) / 1024 * 16);
             sw.rec = reinterpret_cast<int4 *>(base);
             base += align_up(c * 16);
             sw.map_list = reinterpret_cast<int64_t *>(base);
@@ -696,7 +700,7 @@ moc_status_t enqueue_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n
         if (X.on[k]) {
             MOC_CUDA(h, moc::launch_split_records(X.sp[k], X.sw[k], sk));
             MOC_CUDA(h, moc::launch_fwd(X.sp[k], X.mcfg[k], sk));
-            MOC_CUDA(h, moc::launch_split_start(X.sp[k], X.sw[k], sk));
+            MOC_CUDA(h, moc::launch_split_start(X.sp[k], X.sw[k], h->sm_count, sk));
         }
         MOC_CUDA(h, cudaEventRecord(h->bjoin[k], sk));
         MOC_CUDA(h, cudaStreamWaitEvent(st, h->bjoin[k], 0));
@@ -717,19 +721,18 @@ moc_status_t prep_blocks(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
     const size_t blk_bytes = (size_t)(ncell + 1) * p->group_stride * sizeof(float4);
     if ((s = ensure(h, reinterpret_cast<void **>(&h->blk), &h->blk_cap, blk_bytes))) return s;
     if (o->exp_mode == MOC_EXP_TABLE && (s = ensure_table(h, o, st))) return s;
-    const int store = o->precision == MOC_PREC_BF16   ? moc::STORE_BF16
-                      : o->precision == MOC_PREC_FP16 ? moc::STORE_F16
-                                                      : moc::STORE_F32;
-    // the layout the sweep's lanes read (pick_config's groups per lane)
-    const int vec = o->vec ? o->vec : moc::auto_vec(p->n_groups);
-    if (store == moc::STORE_F32)
+    // the layout the sweep's lanes read (its groups per lane and loop)
+    moc::FwdConfig cfg;
+    if ((s = pick_config(h, p, o, &cfg))) return s;
+    if (cfg.store == moc::STORE_F32)
         MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                            p->n_intervals, p->group_stride, o->dz, o->zin,
-                                           o->mu, o->mu2, st, true, moc::f32_pairs(vec)));
+                                           o->mu, o->mu2, st, true, moc::f32_pairs(cfg.vec),
+                                           moc::fwd_bulk(cfg) ? cfg.vec : 0));
     else
-        MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, store, p->n_regions,
-                                             p->n_intervals, p->group_stride, o->dz, o->zin,
-                                             o->mu, o->mu2, st, true));
+        MOC_CUDA(h, moc::launch_prep_block16(p->sigT, p->source, h->blk, cfg.store,
+                                             p->n_regions, p->n_intervals, p->group_stride,
+                                             o->dz, o->zin, o->mu, o->mu2, st, true));
     return MOC_OK;
 }
 
@@ -862,12 +865,12 @@ moc_status_t moc::check_args(const moc_problem_t *p, const moc_fwd_opts_t *o)
     return check_problem(p, o);
 }
 
-bool moc::all_device_accessible(const moc_problem_t *p)
+bool moc::all_device_accessible(const moc_problem_t *p, int dev)
 {
     const void *ptrs[] = {p->track_offsets, p->seg_region, p->seg_interval, p->seg_ds,
                           p->sigT, p->source, p->fine_flux, p->psi};
     for (const void *q : ptrs)
-        if (!device_accessible(q)) return false;
+        if (!device_accessible(q, dev)) return false;
     return true;
 }
 
@@ -989,7 +992,7 @@ moc_status_t moc_attenuate_fwd(moc_handle_t h, const moc_problem_t *p,
     const void *ptrs[] = {p->track_offsets, p->seg_region, p->seg_interval, p->seg_ds,
                           p->sigT, p->source, p->fine_flux, p->psi};
     for (const void *q : ptrs)
-        if (!device_accessible(q)) return MOC_ERR_INVALID_ARG;
+        if (!device_accessible(q, h->device)) return MOC_ERR_INVALID_ARG;
     return fwd_device(h, p, o, static_cast<cudaStream_t>(stream));
 }
 
@@ -1163,7 +1166,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     const void *ptrs[] = {p->track_offsets, p->seg_region, p->seg_interval, p->seg_ds,
                           p->sigT, p->source, p->psi, w, v, d_sigT, d_source, d_psi_in};
     for (const void *ptr : ptrs)
-        if (!device_accessible(ptr)) return MOC_ERR_INVALID_ARG;
+        if (!device_accessible(ptr, h->device)) return MOC_ERR_INVALID_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
@@ -1378,6 +1381,7 @@ moc_status_t moc_synchronize(moc_handle_t h, void *stream)
     MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));
     MOC_CUDA(h, cudaStreamSynchronize(st));
     if (*h->err_host & moc::DEVERR_TRACK) return MOC_ERR_BAD_TRACK;
+    if (*h->err_host & moc::DEVERR_TIMEOUT) return MOC_ERR_DEVICE_TIMEOUT;
     return *h->err_host ? MOC_ERR_BAD_INDEX : MOC_OK;
 }
 

@@ -258,7 +258,7 @@ const void *pick(int vec, int ek)
 int grid_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
-    if (b > 152 * 8) b = 152 * 8;
+    if (b > grid_cap(8)) b = grid_cap(8);
     return (int)(b < 1 ? 1 : b);
 }
 

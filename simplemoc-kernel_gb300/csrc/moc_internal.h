@@ -22,16 +22,26 @@ constexpr bool PAIRED_FP32 = MOC_PAIRED_FP32 != 0;
 constexpr bool f32_pairs(int vec) { return PAIRED_FP32 && vec % 2 == 0; }
 
 // The size / enum / alignment checks of moc_attenuate_fwd, and its check that every
-// problem pointer is device (or managed) memory.
+// problem pointer is memory of device `dev` (or managed memory).
 moc_status_t check_args(const moc_problem_t *p, const moc_fwd_opts_t *o);
-bool all_device_accessible(const moc_problem_t *p);
+bool all_device_accessible(const moc_problem_t *p, int dev);
+
+// Streaming multiprocessors of the current device (queried once per device), for the
+// grid sizes of the grid-stride kernels: at most sm_count * per_sm blocks.
+int current_sm_count();
+inline int64_t grid_cap(int per_sm) { return (int64_t)current_sm_count() * per_sm; }
 
 // Device error bits, OR-ed into the handle's error word by the kernels.
 enum : int32_t {
     DEVERR_OFFSETS = 1,  // a track's [begin, end) is not inside [0, S]
     DEVERR_INDEX = 2,    // a segment's region or interval is out of range
     DEVERR_TRACK = 4,    // track generation: a track record is invalid
+    DEVERR_TIMEOUT = 8,  // a bounded wait on a bulk copy gave up (the sweep stopped)
 };
+
+// SM clocks a warp waits for one bulk copy before it reports DEVERR_TIMEOUT and stops:
+// about a second at GB300 clocks, far beyond any copy's latency.
+constexpr long long BULK_WAIT_LIMIT = 2000000000LL;
 
 // How 1 - exp(-tau) and the cancelling terms are evaluated.
 enum ExpKind : int {
@@ -70,6 +80,7 @@ struct SweepParams {
     int32_t R, I, G, Gs, T, n_chunks;
     int32_t group_major;          // item order: 1 group chunk by group chunk, 0 track by track
     int32_t null_cell;            // R*I when blk has the null-cell row after the cells, else -1
+    int32_t ring_d;               // bulk-copy ring: slots per warp (RD_BULK loop)
     int64_t S, n_items;
     const int64_t *off;
     const int32_t *reg;
@@ -100,7 +111,7 @@ struct SweepParams {
 // Split workspace (device) and the chunk length.
 struct SplitWork {
     int64_t *base;    // [T + 1] first record of each track; base[T] = records
-    int64_t *bsum;    // [ceil(T / 1024)] scan block sums
+    int64_t *bsum;    // [2 * ceil(T / 1024)] scan block sums (records, maps)
     int4 *rec;        // [cap]
     int64_t *map_list;  // [cap] record ids of non-last chunks
     int64_t *n_map;     // number of map items
@@ -116,7 +127,8 @@ int64_t split_max_records(int64_t T, int64_t S, int chunk);
 cudaError_t launch_split_records(const SweepParams &P, const SplitWork &W, cudaStream_t st);
 // psi entering every chunk of the split tracks from the maps: start_0 = psi_in,
 // start_{k+1} = a_k start_k + b_k.
-cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStream_t st);
+cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, int sm_count,
+                               cudaStream_t st);
 
 // Cell blocks of every (region, interval) and group: blk[c][g] = (sigT of the region,
 // q0, q1*mu, q2*mu2), the coefficients rounded exactly as src/cpu/kernel.c:111-191 and
@@ -127,9 +139,14 @@ cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStr
 // (sigT_2h, sigT_2h+1, q0_2h, q0_2h+1) and (q1mu_2h, q1mu_2h+1, q2mu2_2h, q2mu2_2h+1), so
 // that a lane's loads land every pair of operands of the packed arithmetic in adjacent
 // registers (Gs is a multiple of 4, so pairs never straddle cells).
+// strided = VEC > 1 (with pairs): the lane-strided layout of the bulk-copy ring, in which
+// each 32*VEC-group chunk of a row (n float4, n/VEC lanes) holds lane l's k-th float4 of
+// the pair layout at k*(n/VEC) + l, so that a warp's lanes read a slot copied from it
+// with conflict-free 16-byte shared loads.
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st, bool null_row = false, bool pairs = false);
+                              cudaStream_t st, bool null_row = false, bool pairs = false,
+                              int strided = 0);
 // The same blocks rounded to bf16 (store = STORE_BF16) or fp16 (STORE_F16), to nearest.
 cudaError_t launch_prep_block16(const float *sigT, const float *source, void *blk, int store,
                                 int R, int I, int Gs, float dz, float zin, float mu,
@@ -139,8 +156,8 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
                           cudaStream_t st);
 
 // The forward sweep (persistent, one warp per (track, group chunk) work item).
-constexpr int RING_DEPTH = 8;  // depth of the shared-memory prefetch ring
-constexpr int DESC_RING_F4 = 32;  // the branch-free loop's 64 (cell, ds) pairs per warp
+constexpr int RING_MAX = 16;      // most slots of a warp's bulk-copy ring
+constexpr int DESC_RING_F4 = 32;  // a warp's 64 (cell, ds) descriptor pairs
 struct FwdConfig {
     int vec;              // groups per lane: 1, 2, 4
     int warps_per_block;  // 1..16
@@ -148,10 +165,15 @@ struct FwdConfig {
     int blocks;           // grid size (0 = fill the GPU)
     int store = STORE_F32;
     int tally = TALLY_F32;
-    int prefetch = 1;     // 1: registers, one segment ahead; RING_DEPTH: cp.async ring
+    int prefetch = 1;     // 1: registers, one segment ahead; 2..RING_MAX: a ring of that
+                          // many slots in shared memory per warp, filled by bulk copies
+                          // (FP32 blocks in the lane-strided layout, FP32 tallies)
     int mode = 0;         // 0: the sweep; 1: affine maps of split chunks (split mode)
     bool branch_free = false;  // the null-cell row exists and G is a multiple of vec
 };
+// The bulk-copy ring reads FP32 cell blocks in the lane-strided layout (launch_prep_block
+// with strided = vec).
+inline bool fwd_bulk(const FwdConfig &c) { return c.prefetch > 1; }
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &cfg, cudaStream_t st);
 // Dynamic shared memory of a configuration (table of tab_n pairs in table mode + rings).
 size_t fwd_smem_bytes(const FwdConfig &cfg, int tab_n);

@@ -51,59 +51,78 @@ __device__ __forceinline__ int64_t maps_of(int64_t n, int map_all)
     return n > 1 ? (map_all ? n : n - 1) : 0;
 }
 
-// Records and map items of a track, packed for one scan: maps in the high 32 bits,
-// records in the low 32 (both totals stay below 2^31: the host caps them).
-__device__ __forceinline__ int64_t packed_count(int64_t n, int map_all)
+// Records and map items of a track, scanned together as a pair of 64-bit counts (offsets
+// that are not a partition of [0, S] can make either total large; records beyond the
+// workspace are dropped and reported, and neither count can spill into the other).
+struct Counts {
+    int64_t rec, map;
+};
+__device__ __forceinline__ Counts operator+(Counts a, Counts b)
 {
-    return (maps_of(n, map_all) << 32) | n;
+    return Counts{a.rec + b.rec, a.map + b.map};
+}
+__device__ __forceinline__ Counts operator-(Counts a, Counts b)
+{
+    return Counts{a.rec - b.rec, a.map - b.map};
+}
+__device__ __forceinline__ Counts counts_of(int64_t n, int map_all)
+{
+    return Counts{n, maps_of(n, map_all)};
+}
+__device__ __forceinline__ Counts shfl_up(Counts v, int o)
+{
+    return Counts{(int64_t)__shfl_up_sync(FULL, (long long)v.rec, o),
+                  (int64_t)__shfl_up_sync(FULL, (long long)v.map, o)};
 }
 
 // Inclusive scan of v over the block; *total = the block's sum. Called by every thread.
-__device__ int64_t block_incl_scan(int64_t v, int64_t *total)
+__device__ Counts block_incl_scan(Counts v, Counts *total)
 {
-    __shared__ int64_t ws[SCAN_BLOCK / 32];
+    __shared__ Counts ws[SCAN_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int o = 1; o < 32; o <<= 1) {
-        const int64_t u = __shfl_up_sync(FULL, v, o);
-        if (lane >= o) v += u;
+        const Counts u = shfl_up(v, o);
+        if (lane >= o) v = v + u;
     }
     if (lane == 31) ws[w] = v;
     __syncthreads();
     if (w == 0) {
-        int64_t s = lane < nw ? ws[lane] : 0;
+        Counts s = lane < nw ? ws[lane] : Counts{0, 0};
         for (int o = 1; o < 32; o <<= 1) {
-            const int64_t u = __shfl_up_sync(FULL, s, o);
-            if (lane >= o) s += u;
+            const Counts u = shfl_up(s, o);
+            if (lane >= o) s = s + u;
         }
         if (lane < nw) ws[lane] = s;
     }
     __syncthreads();
-    if (w > 0) v += ws[w - 1];
+    if (w > 0) v = v + ws[w - 1];
     *total = ws[nw - 1];
     __syncthreads();  // ws is reused by the next call
     return v;
 }
 
+// W.bsum holds one Counts (two int64) per scan block.
 __global__ void __launch_bounds__(SCAN_BLOCK) scan_sums_kernel(const SweepParams P,
                                                                const SplitWork W)
 {
     const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
-    int64_t total;
-    block_incl_scan(t < P.T ? packed_count(count_of(P, W, t), W.map_all) : 0, &total);
-    if (threadIdx.x == 0) W.bsum[blockIdx.x] = total;
+    Counts total;
+    block_incl_scan(t < P.T ? counts_of(count_of(P, W, t), W.map_all) : Counts{0, 0}, &total);
+    if (threadIdx.x == 0) reinterpret_cast<Counts *>(W.bsum)[blockIdx.x] = total;
 }
 
 // One block: exclusive scan of the nb block sums, in place.
-__global__ void __launch_bounds__(SCAN_BLOCK) scan_bsum_kernel(int64_t *bsum, int64_t nb)
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_bsum_kernel(int64_t *bsum64, int64_t nb)
 {
-    int64_t carry = 0;
+    Counts *bsum = reinterpret_cast<Counts *>(bsum64);
+    Counts carry{0, 0};
     for (int64_t b0 = 0; b0 < nb; b0 += SCAN_BLOCK) {
         const int64_t i = b0 + threadIdx.x;
-        const int64_t v = i < nb ? bsum[i] : 0;
-        int64_t total;
-        const int64_t incl = block_incl_scan(v, &total);
+        const Counts v = i < nb ? bsum[i] : Counts{0, 0};
+        Counts total;
+        const Counts incl = block_incl_scan(v, &total);
         if (i < nb) bsum[i] = carry + incl - v;
-        carry += total;
+        carry = carry + total;
     }
 }
 
@@ -114,13 +133,13 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
 {
     const int64_t t = blockIdx.x * (int64_t)SCAN_BLOCK + threadIdx.x;
     const int64_t n = t < P.T ? count_of(P, W, t) : 0;
-    const int64_t pk = packed_count(n, W.map_all);
-    const int64_t nm = maps_of(n, W.map_all);
-    int64_t total;
-    const int64_t incl = block_incl_scan(pk, &total);
+    const Counts pk = counts_of(n, W.map_all);
+    const int64_t nm = pk.map;
+    Counts total;
+    const Counts incl = block_incl_scan(pk, &total);
     if (t >= P.T) return;
-    const int64_t excl = W.bsum[blockIdx.x] + incl - pk;
-    const int64_t b = excl & 0xffffffffLL, mb = excl >> 32;
+    const Counts excl = reinterpret_cast<const Counts *>(W.bsum)[blockIdx.x] + incl - pk;
+    const int64_t b = excl.rec, mb = excl.map;
     W.base[t] = b;
     if (t == P.T - 1) {
         W.base[P.T] = b + n;
@@ -218,9 +237,10 @@ cudaError_t launch_split_records(const SweepParams &P, const SplitWork &W, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, cudaStream_t st)
+cudaError_t launch_split_start(const SweepParams &P, const SplitWork &W, int sm_count,
+                               cudaStream_t st)
 {
-    split_start_kernel<<<152 * 8, 256, 0, st>>>(P, W);
+    split_start_kernel<<<sm_count * 8, 256, 0, st>>>(P, W);
     return cudaGetLastError();
 }
 

@@ -91,11 +91,12 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     if (cell_groups > MOC_NOALLOC_MAX_CELL_GROUPS) return MOC_ERR_TOO_LARGE;
     if (o->exp_mode == MOC_EXP_TABLE && o->table_points > MOC_NOALLOC_MAX_TABLE_POINTS)
         return MOC_ERR_TOO_LARGE;
-    if (!moc::all_device_accessible(p)) return MOC_ERR_INVALID_ARG;
-
-    std::lock_guard<std::mutex> lock(g_mutex);
     int dev = 0;
     NA_CUDA(cudaGetDevice(&dev));
+    // every array must be memory of the current device (or managed memory)
+    if (!moc::all_device_accessible(p, dev)) return MOC_ERR_INVALID_ARG;
+
+    std::lock_guard<std::mutex> lock(g_mutex);
     unsigned char *base = nullptr;
     int sms = 0;
     if ((s = setup_device(dev, &base, &sms))) return s;
@@ -149,6 +150,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     cfg.warps_per_block =
         o->warps_per_block ? o->warps_per_block : moc::auto_warps_per_block(cfg.exp_kind);
     cfg.prefetch = o->prefetch > 1 ? o->prefetch : 1;
+    if (moc::fwd_bulk(cfg) && cfg.vec > 1 && !moc::f32_pairs(cfg.vec)) return MOC_ERR_UNSUPPORTED;
     const int per_sm = moc::fwd_blocks_per_sm(cfg, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
     cfg.blocks = per_sm * sms;
@@ -159,7 +161,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
 
     NA_CUDA(moc::launch_prep_block(p->sigT, p->source, blk, p->n_regions, p->n_intervals,
                                    p->group_stride, o->dz, o->zin, o->mu, o->mu2, st, false,
-                                   moc::f32_pairs(cfg.vec)));
+                                   moc::f32_pairs(cfg.vec), moc::fwd_bulk(cfg) ? cfg.vec : 0));
     NA_CUDA(moc::launch_fwd(sp, cfg, st));
     return MOC_OK;
 }

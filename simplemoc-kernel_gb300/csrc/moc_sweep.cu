@@ -110,10 +110,12 @@ __global__ void prep_block_kernel(const float *__restrict__ sigT,
 }
 
 // The FP32 blocks in the pair layout: one thread per pair of groups (k, k + 1), k even.
+// svec > 1: in the lane-strided layout of the bulk-copy ring (float4 w of a 32*svec-group
+// chunk of n float4 goes to (w % svec) * (n / svec) + w / svec of the chunk).
 __global__ void prep_pairs_kernel(const float *__restrict__ sigT,
                                   const float *__restrict__ source, float4 *__restrict__ blk,
                                   int R, int I, int Gs, float dz, float zin, float mu,
-                                  float mu2, int null_row)
+                                  float mu2, int null_row, int svec)
 {
     const int64_t n = (int64_t)R * I * Gs;
     const int64_t n_all = n + (null_row ? Gs : 0);
@@ -124,8 +126,19 @@ __global__ void prep_pairs_kernel(const float *__restrict__ sigT,
         const float4 u = k < n ? cell_block(sigT, source, k, I, Gs, dz, zin, mu, mu2) : nul;
         const float4 w =
             k < n ? cell_block(sigT, source, k + 1, I, Gs, dz, zin, mu, mu2) : nul;
-        blk[k] = make_float4(u.x, w.x, u.y, w.y);
-        blk[k + 1] = make_float4(u.z, w.z, u.w, w.w);
+        int64_t d0 = k, d1 = k + 1;
+        if (svec > 1) {
+            const int64_t row = k / Gs;
+            const int g = (int)(k - row * Gs);
+            const int cw = 32 * svec;
+            const int cb = g / cw * cw;                   // the chunk's first group
+            const int nl = min(Gs - cb, cw) / svec;       // lanes the chunk covers
+            const int w0 = g - cb, w1 = w0 + 1;
+            d0 = row * Gs + cb + (w0 % svec) * nl + w0 / svec;
+            d1 = row * Gs + cb + (w1 % svec) * nl + w1 / svec;
+        }
+        blk[d0] = make_float4(u.x, w.x, u.y, w.y);
+        blk[d1] = make_float4(u.z, w.z, u.w, w.w);
     }
 }
 
@@ -236,6 +249,21 @@ __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t 
 
 enum : int { MODE_SWEEP = 0, MODE_MAP = 1 };
 
+// Segment loops of sweep_item (template parameter RD):
+enum : int {
+    RD_REG = 0,       // one segment ahead in registers, checks per segment
+    RD_FREE = -1,     // branch-free windowed pair loop, one segment ahead in registers
+    RD_BULK = -3,     // a ring of P.ring_d slots per warp filled by bulk copies
+};
+
+// A warp's position in its bulk-copy ring, kept across its work items: the slot the next
+// copy goes to (lane 0), the slot and phase parity the next wait is on, and the copies in
+// flight (lane 0).
+struct RingState {
+    int is, cs, inflight;
+    uint32_t ph;
+};
+
 // One work item. Without chunk records an item is (track, group chunk). With records
 // (split mode) it is (record, group chunk): a whole track (psi in place), or a chunk of
 // a split track, which starts from its precomputed psi and, if it is the track's last,
@@ -245,9 +273,11 @@ enum : int { MODE_SWEEP = 0, MODE_MAP = 1 };
 // [0, 32 VEC) first, ...) when P.group_major is set, so the warps in flight read one
 // group chunk's slice of every cell block and tally row, a smaller working set in L2;
 // else track by track. n_units: tracks, records or map items.
+// Returns false when a bounded wait of the bulk-copy ring gave up (the warp stops).
 template <int VEC, int EK, int ST, int TL, int RD, int MODE>
-__device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, int64_t n_units,
-                                           int lane, const TableRef &tr, float4 *ring)
+__device__ __forceinline__ bool sweep_item(const SweepParams &P, int64_t item, int64_t n_units,
+                                           int lane, const TableRef &tr, float4 *ring,
+                                           RingState &rs)
 {
     const int Gs = P.Gs;
     int64_t beg, end, row_q = 0, unit;
@@ -265,18 +295,18 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         int64_t q = unit;
         if constexpr (MODE == MODE_MAP) {
             q = P.map_list[q];
-            if ((uint64_t)q >= (uint64_t)P.rec_cap) return;
+            if ((uint64_t)q >= (uint64_t)P.rec_cap) return true;
         }
         const int4 r = __ldg(P.rec + q);
         const int flags = r.z;
         if constexpr (MODE == MODE_MAP)
-            if (flags & (CHUNK_SINGLE | CHUNK_LAST)) return;
+            if (flags & (CHUNK_SINGLE | CHUNK_LAST)) return true;
         beg = (int64_t)(uint32_t)r.x | ((int64_t)r.y << 32);
         end = beg + (flags & CHUNK_LEN_MASK);
         // records come from offsets that may not be a partition of [0, S]: check them
         if (!(beg >= 0 && end <= P.S && (unsigned)r.w < (unsigned)P.T)) {
             if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
-            return;
+            return true;
         }
         float *track_psi = P.psi + (int64_t)r.w * Gs;
         if (flags & CHUNK_SINGLE) {
@@ -292,7 +322,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         end = P.off[t + 1];
         if (!(beg >= 0 && beg <= end && end <= P.S)) {
             if (lane == 0) atomicOr(P.err, DEVERR_OFFSETS);
-            return;
+            return true;
         }
         psi_in = psi_out = P.psi + (int64_t)t * Gs;
     }
@@ -307,13 +337,13 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
     }
     if (MODE == MODE_SWEEP && act) psi = ld_psi<VEC>(psi_in + g0, nvalid);
 
-    // Descriptor windows: A = segments [wb, wb+32), B = the next 32 (the branch-free loop
-    // keeps them in shared memory instead).
+    // Descriptor windows: A = segments [wb, wb+32), B = the next 32 (the branch-free and
+    // bulk loops keep them in shared memory instead).
     const int none = RD < 0 ? P.null_cell : -1;
     int64_t wb = beg;
     int cA = none, cB = none;
     float dA = 0.0f, dB = 0.0f;
-    if constexpr (RD >= 0) {
+    if constexpr (RD == RD_REG) {
         decode(P, wb + lane, end, none, cA, dA);
         decode(P, wb + 32 + lane, end, none, cB, dB);
     }
@@ -346,7 +376,7 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
         }
     };
 
-    if constexpr (RD < 0) {
+    if constexpr (RD == RD_FREE) {
         // Branch-free segments, one ahead (ping-pong registers), 32-bit indexing inside
         // 32-segment descriptor windows: the pair loop shuffles lanes k and k+1 of window
         // A; only the pair at a full window's end reaches into window B. Segments past the
@@ -435,82 +465,126 @@ __device__ __forceinline__ void sweep_item(const SweepParams &P, int64_t item, i
             }
             step(b1, c1, d1);
         }
-    } else {
-        // RD - 1 segments ahead, through a per-warp ring in shared memory filled by
-        // cp.async: slot s holds the warp's 32*VEC consecutive cell-block entries of the
-        // segment in it, copied coalesced (lane l copies entries l, l+32, ...), so every
-        // 32-byte L2 sector is fetched once; lane l then reads its VEC entries
-        // (l*VEC ... l*VEC+VEC-1) after the wait on its copy groups and a __syncwarp.
-        // The issue pointer runs RD - 1 segments ahead of the compute pointer, inside
-        // descriptor windows A and B.
-        static_assert(ST == STORE_F32 && (RD & (RD - 1)) == 0 && RD <= 16, "ring");
-        const int gw = g0 - lane * VEC;                   // first group of the warp's chunk
-        const int nrow = Gs - gw < 32 * VEC ? Gs - gw : 32 * VEC;  // entries inside the row
-        auto peek = [&](int64_t jj, int &c, float &d) {
-            const int k = (int)(jj - wb);
-            if (k < 32) {
-                c = __shfl_sync(FULL, cA, k);
-                d = __shfl_sync(FULL, dA, k);
-            } else {
-                c = __shfl_sync(FULL, cB, k - 32);
-                d = __shfl_sync(FULL, dB, k - 32);
-            }
-        };
-        const float4 *blk = static_cast<const float4 *>(P.blk) + gw;
-        auto issue = [&](int64_t jj, int slot) {
-            if (jj < end) {
-                int c;
-                float d;
-                peek(jj, c, d);
-                if (c >= 0) {
-#pragma unroll
-                    for (int v = 0; v < VEC; v++) {
-                        const int q = v * 32 + lane;
-                        if (q < nrow) cp_async16(ring + slot * VEC * 32 + q, blk + c * Gs + q);
-                    }
-                }
-            }
-            cp_async_commit();
-        };
-#pragma unroll
-        for (int s = 0; s < RD - 1; s++) issue(beg + s, s);
-        for (int64_t j = beg; j < end; j++) {
-            if (j - wb == 32) {
-                cA = cB;
-                dA = dB;
-                wb += 32;
-                decode(P, wb + 32 + lane, end, none, cB, dB);
-            }
-            const int slot = (int)((j - beg) & (RD - 1));
-            issue(j + RD - 1, (slot + RD - 1) & (RD - 1));
-            cp_async_wait<RD - 1>();
-            __syncwarp();
+    } else if constexpr (RD == RD_BULK) {
+        // P.ring_d slots per warp in shared memory after the descriptor ring, each holding
+        // one segment's cell blocks for the warp's group chunk (nrow float4, copied from
+        // the lane-strided layout with one bulk copy), and one mbarrier per slot. Lane 0
+        // starts the copy of segment j + ring_d - 1 before the warp waits on segment j, so
+        // ring_d - 1 copies are in flight behind the arithmetic. Copies are made only for
+        // segments that name a cell (the null cell included), and each is waited on and
+        // read exactly once, in order, so the copy and wait sides step through the slots
+        // alike; a slot is refilled only after every lane has read it (__syncwarp).
+        static_assert(ST == STORE_F32 && TL == TALLY_F32, "bulk ring: FP32 blocks and tallies");
+        const int D = P.ring_d;
+        float4 *slots = ring + DESC_RING_F4;
+        const uint32_t bar0 = smem_addr(slots + D * 32 * VEC);
+        const int gw = g0 - lane * VEC;                            // the chunk's first group
+        const int nrow = Gs - gw < 32 * VEC ? Gs - gw : 32 * VEC;  // its float4 in a row
+        const uint32_t bytes = (uint32_t)nrow * 16u;
+        const int nl = nrow / VEC;                                 // lanes it covers
+        const int li = lane < nl ? lane : 0;
+        const float4 *src = static_cast<const float4 *>(P.blk) + gw;
+        const int ncell = P.R * P.I;
+        const int lim = act ? ncell : 0;
+        const int gl = act ? g0 : 0;
+        int2 *win = reinterpret_cast<int2 *>(ring);
+        auto put = [&](int64_t w0, int slot0) {
             int c;
             float d;
-            peek(j, c, d);
-            if (c >= 0 && act) {
-                Blk<VEC> b;
-#pragma unroll
-                for (int v = 0; v < VEC; v++) b.v[v] = ring[slot * VEC * 32 + lane * VEC + v];
-                step(b, c, d);
+            decode(P, w0 + lane, end, none, c, d);
+            win[slot0 + lane] = make_int2(c, __float_as_int(d));
+        };
+        auto issue = [&](int pos) {  // lane 0: the copy of the segment at ring position pos
+            const int c = win[pos].x;
+            if (c >= 0) {
+                const uint32_t bar = bar0 + 8u * (uint32_t)rs.is;
+                mbar_expect_tx(bar, bytes);
+                bulk_g2s(smem_addr(slots + rs.is * 32 * VEC), src + (int64_t)c * Gs, bytes, bar);
+                rs.is = rs.is + 1 == D ? 0 : rs.is + 1;
+                rs.inflight++;
             }
-            __syncwarp();  // the slot is refilled by the next iteration's copies
-        }
-        cp_async_wait<0>();
+        };
+        put(beg, 0);
+        put(beg + 32, 32);
         __syncwarp();
+        if (lane == 0) {
+            const int64_t n0 = end - beg < D - 1 ? end - beg : D - 1;
+            for (int s0 = 0; s0 < (int)n0; s0++) issue(s0);
+        }
+        int slot = 0;  // ring position of segment wb
+        for (; wb < end; wb += 32) {
+            const int nk = end - wb < 32 ? (int)(end - wb) : 32;
+            for (int k = 0; k < nk; k++) {
+                if (lane == 0 && wb + k + D - 1 < end) issue((slot + k + D - 1) & 63);
+                const int2 q = win[(slot + k) & 63];
+                const int c = q.x;
+                if (c >= 0) {
+                    const bool ok = mbar_wait_bounded(bar0 + 8u * (uint32_t)rs.cs, rs.ph,
+                                                      BULK_WAIT_LIMIT);
+                    if (!__all_sync(FULL, ok)) {
+                        // give up: report, let the copies in flight land (bounded), stop
+                        if (lane == 0) {
+                            atomicOr(P.err, DEVERR_TIMEOUT);
+                            int cs = rs.cs;
+                            uint32_t ph = rs.ph;
+                            for (int m = 0; m < rs.inflight; m++) {
+                                mbar_wait_bounded(bar0 + 8u * (uint32_t)cs, ph, BULK_WAIT_LIMIT);
+                                if (++cs == D) {
+                                    cs = 0;
+                                    ph ^= 1u;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                        return false;
+                    }
+                    const float4 *sl = slots + rs.cs * 32 * VEC;
+                    Blk<VEC> b;
+#pragma unroll
+                    for (int v = 0; v < VEC; v++) b.v[v] = sl[v * nl + li];
+                    if (++rs.cs == D) {
+                        rs.cs = 0;
+                        rs.ph ^= 1u;
+                    }
+                    if (lane == 0) rs.inflight--;
+                    Vec<VEC> tally, p;
+                    attenuate<VEC, EK>(b, __int_as_float(q.y), P.weight, tr, psi, tally, p);
+                    if constexpr (MODE == MODE_MAP) {
+#pragma unroll
+                        for (int v = 0; v < VEC; v++) amul.v[v] *= p.v[v];
+                    } else {
+                        if (nvalid >= VEC || !act)
+                            red_row_if<VEC>(P.ff + c * Gs + gl, tally, c, lim);
+                        else if ((unsigned)c < (unsigned)ncell)
+                            red_row<VEC>(P.ff + c * Gs + g0, tally, nvalid);
+                    }
+                }
+                __syncwarp();  // every lane has read the slot before it is refilled
+            }
+            put(wb + 64, slot);
+            __syncwarp();
+            slot ^= 32;
+        }
     }
-    if (!act) return;
+    if (!act) return true;
     if constexpr (MODE == MODE_MAP) {
         st_psi<VEC>(P.map_a + row_q + g0, amul, nvalid);
         st_psi<VEC>(P.map_b + row_q + g0, psi, nvalid);
     } else {
         if (psi_out) st_psi<VEC>(psi_out + g0, psi, nvalid);
     }
+    return true;
 }
 
-// Dynamic shared memory: the exponential table (table mode), then one prefetch ring of
-// RD * VEC * 32 float4 per warp (RD > 0) or one 64-segment descriptor ring per warp
-// (RD < 0).
+// Per-warp shared memory of the bulk-copy ring (float4): the descriptor ring, d slots of
+// 32*vec float4, and d 8-byte mbarriers.
+__host__ __device__ inline int bulk_warp_f4(int d, int vec)
+{
+    return DESC_RING_F4 + d * 32 * vec + (8 * d + 15) / 16;
+}
+
+// Dynamic shared memory: the exponential table (table mode), then per warp its 64-segment
+// descriptor ring (RD < 0), followed by its bulk-copy slots and barriers (RD_BULK).
 template <int VEC, int EK, int ST, int TL, int RD, int MODE>
 __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
 {
@@ -523,12 +597,22 @@ __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
         __syncthreads();
         tr = TableRef{s_tab, P.tab_n, P.tab_dx, P.tab_max};
     }
-    float4 *ring = nullptr;  // the warp's prefetch ring, or its descriptor ring (RD < 0)
-    if constexpr (RD != 0) {
-        const int tab_f4 = EK == EXPK_TABLE ? (P.tab_n + 1) / 2 : 0;
-        ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * (RD > 0 ? RD * VEC * 32 : DESC_RING_F4);
-    }
     const int lane = threadIdx.x & 31;
+    float4 *ring = nullptr;  // the warp's descriptor ring (and bulk-copy slots)
+    RingState rs{0, 0, 0, 0u};
+    if constexpr (RD != RD_REG) {
+        const int tab_f4 = EK == EXPK_TABLE ? (P.tab_n + 1) / 2 : 0;
+        const int per_warp = RD == RD_BULK ? bulk_warp_f4(P.ring_d, VEC) : DESC_RING_F4;
+        ring = s_dyn + tab_f4 + (threadIdx.x >> 5) * per_warp;
+    }
+    if constexpr (RD == RD_BULK) {
+        if (lane == 0) {
+            const uint32_t bar0 = smem_addr(ring + DESC_RING_F4 + P.ring_d * 32 * VEC);
+            for (int d = 0; d < P.ring_d; d++) mbar_init(bar0 + 8u * (uint32_t)d, 1);
+            mbar_init_fence();
+        }
+        __syncwarp();
+    }
     int64_t n_items = P.n_items, n_units = P.T;
     if (P.rec) {
         const int64_t n = MODE == MODE_MAP ? *P.n_map : *P.n_rec;
@@ -541,14 +625,17 @@ __global__ void __launch_bounds__(512) fwd_kernel(const SweepParams P)
         const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
         for (int64_t item = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
              item < n_items; item += nw)
-            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, n_units, lane, tr, ring);
+            if (!sweep_item<VEC, EK, ST, TL, RD, MODE>(P, item, n_units, lane, tr, ring, rs))
+                break;
     } else {
         for (;;) {
             unsigned long long item = 0;
             if (lane == 0) item = atomicAdd(P.counter, 1ULL);
             item = __shfl_sync(FULL, item, 0);
             if (item >= (unsigned long long)n_items) break;
-            sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, n_units, lane, tr, ring);
+            if (!sweep_item<VEC, EK, ST, TL, RD, MODE>(P, (int64_t)item, n_units, lane, tr,
+                                                       ring, rs))
+                break;
         }
     }
 }
@@ -581,47 +668,46 @@ __global__ void finish_kernel(float *__restrict__ ff, const float *__restrict__ 
     }
 }
 
-template <int VEC, int EK, int ST, int TL, int RD = 0, int MODE = MODE_SWEEP>
+template <int VEC, int EK, int ST, int TL, int RD = RD_REG, int MODE = MODE_SWEEP>
 const void *fwd_fn()
 {
     return reinterpret_cast<const void *>(&fwd_kernel<VEC, EK, ST, TL, RD, MODE>);
 }
 
-// The register-prefetch loop: the branch-free windowed pair loop (RD = -1) where the
+// The register-prefetch loop: the branch-free windowed pair loop (RD_FREE) where the
 // configuration allows it (a null-cell row, G a multiple of VEC), else the ping-pong loop
-// with per-segment checks (RD = 0).
+// with per-segment checks (RD_REG).
 template <int VEC, int EK, int ST, int TL, int MODE = MODE_SWEEP>
 const void *reg_fn(bool branch_free)
 {
-    return branch_free ? fwd_fn<VEC, EK, ST, TL, -1, MODE>()
-                       : fwd_fn<VEC, EK, ST, TL, 0, MODE>();
+    return branch_free ? fwd_fn<VEC, EK, ST, TL, RD_FREE, MODE>()
+                       : fwd_fn<VEC, EK, ST, TL, RD_REG, MODE>();
 }
 
-// The instantiated (exp, storage, tally, prefetch) combinations, for every VEC:
-//   plain FP32 / table FP32 with FP32 atomics (the drop-in), register or ring prefetch,
-//   stable math with FP32 storage and all three tally kinds (FP32 tallies also with the
-//   ring), stable math with BF16 / FP16 storage and all three tally kinds.
+// FP32 cell blocks with FP32 tallies: the register loops, or the bulk-copy ring
+// (c.prefetch > 1).
+template <int V, int EK, int MODE>
+const void *f32_fn(const FwdConfig &c)
+{
+    if (fwd_bulk(c)) return fwd_fn<V, EK, STORE_F32, TALLY_F32, RD_BULK, MODE>();
+    return reg_fn<V, EK, STORE_F32, TALLY_F32, MODE>(c.branch_free);
+}
+
+// The instantiated (exp, storage, tally, loop) combinations, for every VEC:
+//   plain FP32 / table FP32 / stable FP32 with FP32 atomics: every loop (f32_fn);
+//   stable math with FP32 storage and compensated or FP64 tallies, and stable math with
+//   BF16 / FP16 storage and all three tally kinds: the register loops.
 template <int V>
 const void *pick_vec(const FwdConfig &c)
 {
-    if (c.mode == MODE_MAP) {  // maps: no tallies; FP32 storage may use the ring
-        if (c.prefetch == RING_DEPTH) {
-            if (c.store != STORE_F32) return nullptr;
-            if (c.exp_kind == EXPK_PLAIN)
-                return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
-            if (c.exp_kind == EXPK_TABLE)
-                return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
-            return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, RING_DEPTH, MODE_MAP>();
-        }
-        if (c.prefetch != 1) return nullptr;
+    const bool plain_loops = !fwd_bulk(c);
+    if (c.mode == MODE_MAP) {  // maps: no tallies
         if (c.store == STORE_F32) {
-            if (c.exp_kind == EXPK_PLAIN)
-                return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
-            if (c.exp_kind == EXPK_TABLE)
-                return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
-            return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, MODE_MAP>(c.branch_free);
+            if (c.exp_kind == EXPK_PLAIN) return f32_fn<V, EXPK_PLAIN, MODE_MAP>(c);
+            if (c.exp_kind == EXPK_TABLE) return f32_fn<V, EXPK_TABLE, MODE_MAP>(c);
+            return f32_fn<V, EXPK_STABLE, MODE_MAP>(c);
         }
-        if (c.exp_kind != EXPK_STABLE) return nullptr;
+        if (c.exp_kind != EXPK_STABLE || !plain_loops) return nullptr;
         if (c.store == STORE_BF16)
             return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32, MODE_MAP>(c.branch_free);
         if (c.store == STORE_F16)
@@ -629,28 +715,17 @@ const void *pick_vec(const FwdConfig &c)
         return nullptr;
     }
     if (c.mode != MODE_SWEEP) return nullptr;
-    if (c.prefetch > 1) {
-        if (c.prefetch != RING_DEPTH || c.store != STORE_F32 || c.tally != TALLY_F32)
-            return nullptr;
-        if (c.exp_kind == EXPK_PLAIN)
-            return fwd_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32, RING_DEPTH>();
-        if (c.exp_kind == EXPK_TABLE)
-            return fwd_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32, RING_DEPTH>();
-        return fwd_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32, RING_DEPTH>();
+    if (c.store == STORE_F32 && c.tally == TALLY_F32) {
+        if (c.exp_kind == EXPK_PLAIN) return f32_fn<V, EXPK_PLAIN, MODE_SWEEP>(c);
+        if (c.exp_kind == EXPK_TABLE) return f32_fn<V, EXPK_TABLE, MODE_SWEEP>(c);
+        return f32_fn<V, EXPK_STABLE, MODE_SWEEP>(c);
     }
+    if (c.exp_kind != EXPK_STABLE || !plain_loops) return nullptr;
     if (c.store == STORE_F32) {
-        if (c.exp_kind == EXPK_PLAIN && c.tally == TALLY_F32)
-            return reg_fn<V, EXPK_PLAIN, STORE_F32, TALLY_F32>(c.branch_free);
-        if (c.exp_kind == EXPK_TABLE && c.tally == TALLY_F32)
-            return reg_fn<V, EXPK_TABLE, STORE_F32, TALLY_F32>(c.branch_free);
-        if (c.exp_kind == EXPK_STABLE) {
-            if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F32>(c.branch_free);
-            if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>(c.branch_free);
-            if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>(c.branch_free);
-        }
+        if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_COMP>(c.branch_free);
+        if (c.tally == TALLY_F64) return reg_fn<V, EXPK_STABLE, STORE_F32, TALLY_F64>(c.branch_free);
         return nullptr;
     }
-    if (c.exp_kind != EXPK_STABLE) return nullptr;
     if (c.store == STORE_BF16) {
         if (c.tally == TALLY_F32) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_F32>(c.branch_free);
         if (c.tally == TALLY_COMP) return reg_fn<V, EXPK_STABLE, STORE_BF16, TALLY_COMP>(c.branch_free);
@@ -674,22 +749,44 @@ const void *pick(const FwdConfig &c)
 
 }  // namespace
 
+int current_sm_count()
+{
+    constexpr int MAX_DEV = 64;
+    static int cached[MAX_DEV] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            n < 1) {
+            cudaGetLastError();
+            return 1;
+        }
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 static int grid_for(int64_t n)
 {
     int64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > grid_cap(16)) blocks = grid_cap(16);
     return (int)(blocks < 1 ? 1 : blocks);
 }
 
 cudaError_t launch_prep_block(const float *sigT, const float *source, float4 *blk, int R,
                               int I, int Gs, float dz, float zin, float mu, float mu2,
-                              cudaStream_t st, bool null_row, bool pairs)
+                              cudaStream_t st, bool null_row, bool pairs, int strided)
 {
     const int64_t n = (int64_t)R * I * Gs + (null_row ? Gs : 0);
     if (n == 0) return cudaSuccess;
+    if (strided > 1 && !pairs) return cudaErrorInvalidValue;
     if (pairs)  // n is a multiple of Gs, itself a multiple of 4: whole pairs
         prep_pairs_kernel<<<grid_for(n / 2), 256, 0, st>>>(sigT, source, blk, R, I, Gs, dz,
-                                                            zin, mu, mu2, null_row);
+                                                            zin, mu, mu2, null_row, strided);
     else
         prep_block_kernel<STORE_F32><<<grid_for(n), 256, 0, st>>>(sigT, source, blk, R, I, Gs,
                                                                    dz, zin, mu, mu2, null_row);
@@ -724,8 +821,8 @@ cudaError_t launch_finish(float *ff, const float *lo, const double *ff64, int64_
 size_t fwd_smem_bytes(const FwdConfig &c, int tab_n)
 {
     size_t b = c.exp_kind == EXPK_TABLE ? (size_t)(tab_n + 1) / 2 * sizeof(float4) : 0;
-    if (c.prefetch == RING_DEPTH)
-        b += (size_t)c.warps_per_block * c.prefetch * c.vec * 32 * sizeof(float4);
+    if (fwd_bulk(c))
+        b += (size_t)c.warps_per_block * bulk_warp_f4(c.prefetch, c.vec) * sizeof(float4);
     else if (c.branch_free)
         b += (size_t)c.warps_per_block * DESC_RING_F4 * sizeof(float4);
     return b;
@@ -735,6 +832,7 @@ int fwd_blocks_per_sm(const FwdConfig &c, int tab_n)
 {
     const void *fn = pick(c);
     if (!fn || c.warps_per_block < 1 || c.warps_per_block > 16) return 0;
+    if (c.prefetch < 1 || c.prefetch > RING_MAX) return 0;
     const size_t smem = fwd_smem_bytes(c, tab_n);
     int n = 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -749,13 +847,15 @@ int fwd_blocks_per_sm(const FwdConfig &c, int tab_n)
 cudaError_t launch_fwd(const SweepParams &p, const FwdConfig &c, cudaStream_t st)
 {
     const void *fn = pick(c);
-    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 16 || c.blocks < 1)
+    if (!fn || c.warps_per_block < 1 || c.warps_per_block > 16 || c.blocks < 1 ||
+        c.prefetch < 1 || c.prefetch > RING_MAX)
         return cudaErrorInvalidValue;
     const size_t smem = fwd_smem_bytes(c, p.tab_n);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     SweepParams copy = p;
+    copy.ring_d = fwd_bulk(c) ? c.prefetch : 0;
     void *args[] = {&copy};
     return cudaLaunchKernel(fn, dim3(c.blocks), dim3(c.warps_per_block * 32), args, smem, st);
 }
@@ -765,7 +865,7 @@ cudaError_t launch_check(const SweepParams &p, cudaStream_t st)
     int64_t work = p.S > p.T ? p.S : p.T;
     int blocks = (int)((work + 255) / 256);
     if (blocks < 1) blocks = 1;
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > grid_cap(8)) blocks = (int)grid_cap(8);
     check_kernel<<<blocks, 256, 0, st>>>(p);
     return cudaGetLastError();
 }

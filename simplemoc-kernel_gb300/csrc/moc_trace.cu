@@ -457,7 +457,7 @@ __global__ void scan_add_kernel(int64_t *x, int64_t n, const int64_t *tile_sum)
 int grid_tracks(int64_t T)
 {
     int64_t b = (T + 255) / 256;
-    if (b > 152 * 64) b = 152 * 64;
+    if (b > grid_cap(64)) b = grid_cap(64);
     return (int)(b < 1 ? 1 : b);
 }
 
@@ -522,7 +522,7 @@ cudaError_t launch_trace_compact(const moc_track_t *tr, int64_t T, const int64_t
 {
     if (T == 0) return cudaSuccess;
     int64_t blocks = (T + 7) / 8;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > grid_cap(16)) blocks = grid_cap(16);
     trace_compact_kernel<<<(unsigned)blocks, 256, 0, st>>>(tr, T, bnd, off, sreg, sitv, sds,
                                                            reg, itv, ds);
     return cudaGetLastError();

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) source_update_kernel(
 int grid_for(int64_t n, int per)
 {
     int64_t b = (n + per - 1) / per;
-    if (b > 152 * 16) b = 152 * 16;
+    if (b > grid_cap(16)) b = grid_cap(16);
     return (int)(b < 1 ? 1 : b);
 }
 

@@ -41,7 +41,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_library_loads_and_reports_version():
     L = mocatt.lib()
-    assert L.moc_abi_version() == 3
+    assert L.moc_abi_version() == 4
     assert L.moc_status_string(mocatt.MOC_ERR_BAD_INDEX).decode().startswith("segment")
     assert L.moc_status_string(999) == b"unknown status"
 

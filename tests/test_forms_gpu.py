@@ -99,10 +99,16 @@ REPORT_FORMS = {
     "plain_fp32": (mocatt.MOC_PREC_FP32, mocatt.MOC_TALLY_ATOMIC_FP32),
     "fp32_stable": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_ATOMIC_FP32),
     "fp32_stable_compensated": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_COMPENSATED),
+    "fp32_stable_fp64": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_FP64),
     "bf16_stable": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_ATOMIC_FP32),
     "bf16_stable_compensated": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_COMPENSATED),
     "fp16_stable": (mocatt.MOC_PREC_FP16, mocatt.MOC_TALLY_ATOMIC_FP32),
 }
+# The accuracy rule of the precision forms: normwise relative error <= 1e-5 for psi and for
+# fine_flux, and RMS relative error <= 1e-5 for psi, against the FP64 oracle on the values
+# the form stores. (Maximum relative errors are printed beside it: single outputs that are
+# sums which cancel can exceed 1e-5 while staying inside the FP32 companion bound.)
+NORMWISE_TOL = 1e-5
 
 
 def test_forms_accuracy_report(handle):
@@ -148,3 +154,67 @@ def test_precision_forms_reject_table_mode(handle):
     st = mocatt.lib().moc_attenuate_fwd(handle.ptr, mocatt.C.byref(dp.c_struct()),
                                         mocatt.C.byref(o), None)
     assert st == mocatt.MOC_ERR_UNSUPPORTED
+
+
+def test_forms_widetau_50M_g128_full_size(cuda):
+    """Every precision form on the wide-tau workload at its stated size (50,000,000
+    segments x 128 groups, 100,000 tracks, 10,000 regions; sigT ~ logU(1e-3, 20),
+    ds ~ U(1e-3, 2)), against the FP64 oracle on the values each form stores (one oracle
+    run per storage kind). Prints max, RMS and normwise relative errors of psi and
+    fine_flux; the stable forms must meet the normwise rule, every form the FP32
+    companion bound. With MOC_FORMS_REPORT=<path> the numbers are written there as JSON."""
+    import json
+    import os
+
+    import torch
+
+    h = mocatt.Handle(0)
+    hp = mocatt.generate(mocatt.WORKLOADS["widetau_50M_g128"])
+    dp = mocatt.DeviceProblem(hp)
+    psi0 = dp.psi.clone()
+    threads = os.cpu_count() or 1
+    outs = {}
+    for name, (prec, tally) in REPORT_FORMS.items():
+        dp.psi.copy_(psi0)
+        dp.fine_flux.zero_()
+        h.fwd(dp, mocatt.default_opts(precision=prec, tally=tally))
+        assert h.synchronize() == 0, name
+        outs[name] = (dp.to_host("psi"), dp.to_host("fine_flux"))
+    h.close()
+    del dp
+    torch.cuda.empty_cache()
+    storage = {mocatt.MOC_PREC_FP32: "fp32", mocatt.MOC_PREC_FP32_STABLE: "fp32",
+               mocatt.MOC_PREC_BF16: "bf16", mocatt.MOC_PREC_FP16: "fp16"}
+    report_all = {}
+    for kind, prec in (("fp32", mocatt.MOC_PREC_FP32_STABLE), ("bf16", mocatt.MOC_PREC_BF16),
+                       ("fp16", mocatt.MOC_PREC_FP16)):
+        qp, coef = oracle.quantized_inputs(hp, prec)
+        ref = oracle.fwd_fp64_coef(qp, coef, threads=threads)
+        for name, (p_, _) in REPORT_FORMS.items():
+            if storage[p_] != kind:
+                continue
+            psi, ff = outs.pop(name)
+            rep = report(hp, psi, ff, ref)
+            res = parity.check_plain(psi, ff, ref, hp.G)
+            report_all[name] = {k: {"max_rel": v[0], "rms_rel": v[1], "normwise": v[2]}
+                                for k, v in (("psi", rep["psi"]), ("fine_flux", rep["ff"]))}
+            report_all[name]["bound_ratio"] = res
+        del ref
+    report_all["inputs"] = ("widetau_50M_g128 at full size: 50,000,000 segments x 128 groups, "
+                            "100,000 tracks, 10,000 regions x 5 intervals, sigT ~ logU(1e-3, 20), "
+                            "ds ~ U(1e-3, 2), seed 2; FP64 oracle on the stored (rounded) sigT "
+                            "and coefficients; relative error floor 1e-6 of the RMS")
+    print(json.dumps(report_all, indent=1))
+    path = os.environ.get("MOC_FORMS_REPORT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(report_all, f, indent=1)
+    for name, (prec, _) in REPORT_FORMS.items():
+        if prec == mocatt.MOC_PREC_FP32:
+            continue
+        r = report_all[name]
+        assert r["psi"]["normwise"] <= NORMWISE_TOL, (name, r)
+        assert r["fine_flux"]["normwise"] <= NORMWISE_TOL, (name, r)
+        assert r["psi"]["rms_rel"] <= NORMWISE_TOL, (name, r)
+    # the reference's expressions fail the rule on these inputs; the stable ones meet it
+    assert report_all["plain_fp32"]["psi"]["rms_rel"] > 10 * report_all["fp32_stable"]["psi"]["rms_rel"]
