@@ -174,20 +174,31 @@ def load_peaks() -> dict:
 
 
 def run_peaks() -> dict:
+    """The roofline microbenchmarks (csrc/moc_peaks.cu) on GPU 0, with the SM clock sampled
+    by nvidia-smi while they run and the date of the run."""
     lib = C.CDLL(os.path.join(PKG, "_build", "libmocpeaks.so"))
     lib.mocpeak_run.restype = C.c_int
-    res = (C.c_double * 10)()
-    rc = lib.mocpeak_run(res, 10)
+    res = (C.c_double * 14)()
+    clocks = ClockSampler(0)
+    rc = lib.mocpeak_run(res, 14)
+    clk = clocks.stop()
     if rc:
         raise RuntimeError(f"mocpeak_run failed: {rc}")
     out = {"l2_stream_read_gbs": res[0], "l2_row_gather_hashed_gbs": res[1],
            "l2_row_reduce_hashed_gbs": res[2], "fp32_fma_tflops": res[3],
            "mufu_ex2_gops": res[4], "hbm_read_gbs": res[5], "l2_row_gather_gbs": res[6],
            "l2_row_reduce_gbs": res[7], "l2_mix_gbs": res[8], "fp64_fma_tflops": res[9],
+           "l2_wide_gather_gbs": res[10], "l2_wide_reduce_gbs": res[11],
+           "l2_wide_mix_gbs": res[12], "fp32_fma2_tflops": res[13],
            "mix": "four random 512-byte row gathers per 512-byte red.v4 row reduction "
                   "(the sweep's 16 B gathered : 4 B reduced per segment*group)",
+           "wide_mix": "the sweep's shape at its most parallel: eight streams per warp, each a "
+                       "random 1 KB row read with one 256-bit load per lane and a random "
+                       "256-byte row reduced with red.v2 (16 B : 4 B per segment*group), best "
+                       "of 8, 16 and 24 warps per SM",
            "how": "simplemoc-kernel_gb300/csrc/moc_peaks.cu via bench.py --peaks: "
-                  "CUDA events, mean of 5 launches after 1 warm-up"}
+                  "CUDA events, mean of 5 launches after 1 warm-up",
+           "clocks": clk, "date": time.strftime("%Y-%m-%d %H:%M:%S UTC", time.gmtime())}
     return out
 
 
@@ -218,6 +229,105 @@ def config_of(args, w) -> dict:
             "exp_mode": args.exp, "form": "plain FP32 (reference computation, drop-in)",
             "l2": "flushed between steps (256 MiB write); 0.5 GB of descriptors per step "
                   "exceeds L2", "parallelism": "replicas only (one sweep per GPU)"}
+
+
+def survey_bytes_per_unit(I: int, G: int) -> float:
+    """L2 bytes per segment*group of the reference's own access pattern: sigT 4 B, the
+    source rows the axial fit reads (two at the first and last interval, three inside:
+    4 (2*2 + 3*(I-2)) / I B), the tally 4 B, and an 8-byte descriptor per segment (8/G).
+    At I = 5, G = 128: 18.46 B."""
+    return 4.0 + 4.0 * (2 * 2 + 3 * (I - 2)) / I + 4.0 + 8.0 / G
+
+
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "sweep_fwd_50M_g128_traffic.json")
+
+
+def sweep_roofline(hp, sweep_ms: float, prep_ms: float, split_ms: float) -> dict:
+    """The sweep kernel against the measured peaks. achieved = algorithmic L2 bytes per
+    launch / the kernel's mean event time, in two byte models: the reference's access
+    pattern (18.46 B per segment*group at 50M x 128) and this layout's (the 16-byte cell
+    block + descriptors + the 4-byte tally, 20.07 B). peak = the stronger of the two
+    measured gather+reduction mixes (profiles/peaks_gb300.json, bench.py --peaks). The other
+    resources (FP32, MUFU, HBM) are timed at their measured peaks; the largest binds."""
+    peaks = load_peaks()
+    units = float(hp.S) * hp.G
+    sweep_s = sweep_ms * 1e-3
+    per = l2_bytes_per_unit(hp.I, hp.G)
+    layout_b = per["gather"] + per["reduce"]
+    survey_b = survey_bytes_per_unit(hp.I, hp.G)
+    roof = {"bound": "l2", "unit": "GB/s",
+            "achieved": survey_b * units / sweep_s / 1e9,
+            "algorithmic_bytes_per_unit": survey_b,
+            "bytes_model": "the reference's access pattern: sigT + the fit's source rows + "
+                           "tally + descriptor (18.46 B per segment*group at 50M x 128)",
+            "achieved_layout": layout_b * units / sweep_s / 1e9,
+            "layout_bytes_per_unit": layout_b,
+            "units_per_launch": units, "sweep_ms": sweep_ms, "prep_ms": prep_ms,
+            "split_ms": split_ms, "traffic": None}
+    mixes = {k: peaks[k] for k in ("l2_mix_gbs", "l2_wide_mix_gbs") if peaks.get(k)}
+    terms = {}
+    if mixes:
+        key = max(mixes, key=mixes.get)
+        roof["peak"] = mixes[key]
+        roof["peak_source"] = (f"profiles/peaks_gb300.json {key} (bench.py --peaks, "
+                               f"csrc/moc_peaks.cu), measured {peaks.get('date', 'undated')}"
+                               f" at SM clock {peaks.get('clocks', {}).get('sm_mhz')} MHz")
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof["frac_layout"] = roof["achieved_layout"] / roof["peak"]
+        terms["l2"] = survey_b * units / (roof["peak"] * 1e9) * 1e3
+        fp32 = max(peaks.get("fp32_fma_tflops", 0.0), peaks.get("fp32_fma2_tflops", 0.0))
+        terms["fp32"] = FP32_OPS_PER_UNIT * units / (fp32 * 1e12 / 2) * 1e3
+        terms["mufu"] = MUFU_OPS_PER_UNIT * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3
+    else:
+        roof["peak"] = None
+        roof["frac"] = None
+    hbm_bytes = hbm_compulsory_bytes(hp)
+    terms["hbm"] = hbm_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
+    roof["terms_ms"] = terms
+    binding = max(terms, key=terms.get)
+    roof["binding_term"] = binding
+    roof["binding_frac"] = terms[binding] / sweep_ms
+    roof["hbm"] = {"compulsory_bytes": hbm_bytes, "achieved_gbs": hbm_bytes / sweep_s / 1e9,
+                   "peak_gbs": peaks["hbm_gbs"], "frac": hbm_bytes / sweep_s / 1e9 / peaks["hbm_gbs"],
+                   "peak_source": peaks["hbm_source"]}
+    if os.path.exists(TRAFFIC_FILE) and hp.S == 50_000_000 and hp.G == 128:
+        with open(TRAFFIC_FILE) as f:
+            tr = json.load(f)
+        roof["traffic"] = tr.get("dram_bytes_per_launch")
+        roof["traffic_source"] = {k: tr.get(k) for k in ("kernel", "captured", "command",
+                                                         "lts_bytes_per_launch")}
+    return roof
+
+
+def plain_timing(h, dp, hp, opts, steps: int, flush, stream) -> dict:
+    """A plain-form sweep timed as the headline is: 3 warm-up calls, then `steps` calls each
+    after an L2 flush, CUDA events around each call on its stream, the sweep kernel's own
+    events inside the library."""
+    import torch
+
+    units = float(hp.S) * hp.G
+    for _ in range(3):
+        h.fwd(dp, opts, stream)
+    if h.synchronize(stream):
+        raise RuntimeError("device error")
+    step_ms, sweep_ms = [], []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.fwd(dp, opts, stream)
+        e1.record(stream)
+        t = h.timings()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        sweep_ms.append(t.sweep_ms)
+    if h.synchronize(stream):
+        raise RuntimeError("device error")
+    ms = statistics.mean(step_ms)
+    return {"segments": hp.S, "groups": hp.G, "tracks": hp.T, "regions": hp.R,
+            "ms_per_step": ms, "sweep_ms": statistics.mean(sweep_ms),
+            "value": units / (ms * 1e-3), "unit": UNIT, "steps": steps}
 
 
 def gpu_arm(args, workload):
@@ -313,44 +423,8 @@ def gpu_arm(args, workload):
         return
 
     # ---- roofline of the sweep kernel ----------------------------------------------
-    peaks = load_peaks()
-    sweep_s = statistics.mean(sweep_ms) * 1e-3
-    per = l2_bytes_per_unit(hp.I, hp.G)
-    l2_bytes = (per["gather"] + per["reduce"]) * units
-    roof = {"bound": "l2", "unit": "GB/s",
-            "achieved": l2_bytes / sweep_s / 1e9,
-            "algorithmic_bytes_per_unit": per["gather"] + per["reduce"],
-            "units_per_launch": units, "sweep_ms": sweep_s * 1e3,
-            "prep_ms": statistics.mean(prep_ms), "split_ms": statistics.mean(split_ms),
-            "traffic": None}
-    terms = {}
-    if "l2_mix_gbs" in peaks:
-        # every resource the sweep needs, at its measured peak; the largest time binds
-        terms["l2"] = l2_bytes / (peaks["l2_mix_gbs"] * 1e9) * 1e3
-        terms["fp32"] = FP32_OPS_PER_UNIT * units / (peaks["fp32_fma_tflops"] * 1e12 / 2) * 1e3
-        terms["mufu"] = MUFU_OPS_PER_UNIT * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3
-        roof["peak"] = peaks["l2_mix_gbs"]
-        roof["peak_source"] = ("profiles/peaks_gb300.json l2_mix_gbs: random 512-byte row "
-                               "gathers and red.v4 row reductions in the sweep's 4:1 byte mix "
-                               "(bench.py --peaks, csrc/moc_peaks.cu)")
-    hbm_bytes = hbm_compulsory_bytes(hp)
-    terms["hbm"] = hbm_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
-    roof["terms_ms"] = terms
-    binding = max(terms, key=terms.get)
-    roof["binding_term"] = binding
-    roof["binding_frac"] = terms[binding] / (sweep_s * 1e3)
-    if roof.get("peak"):
-        roof["frac"] = roof["achieved"] / roof["peak"]
-    else:
-        roof["peak"] = None
-        roof["frac"] = None
-    roof["hbm"] = {"compulsory_bytes": hbm_bytes, "achieved_gbs": hbm_bytes / sweep_s / 1e9,
-                   "peak_gbs": peaks["hbm_gbs"], "frac": hbm_bytes / sweep_s / 1e9 / peaks["hbm_gbs"],
-                   "peak_source": peaks["hbm_source"]}
-    prof = os.path.join(ROOT, "profiles", "sweep_fwd_50M_g128_traffic.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            roof["traffic"] = json.load(f).get("dram_bytes_per_launch")
+    roof = sweep_roofline(hp, statistics.mean(sweep_ms), statistics.mean(prep_ms),
+                          statistics.mean(split_ms))
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -361,8 +435,22 @@ def gpu_arm(args, workload):
         "config": config_of(args, workload), "roofline": roof, "e2e": e2e,
         "gpu_launches": launches, "clocks": clk,
     }
+    if ws == 1 and args.exp == "full" and not args.no_extra:
+        # the other plain-form lines: the table exp mode on this workload, and the
+        # reference's CPU-sized problem (1M segments x 64 groups)
+        line["table"] = plain_timing(h, dp, hp, mocatt.default_opts(
+            profile=1, exp_mode=mocatt.MOC_EXP_TABLE, table_points=args.table_points,
+            table_max=10.0), args.steps, flush, stream)
+        line["table"].update(workload=workload.name, exp_mode="table",
+                             table_points=args.table_points, table_max=10.0)
+        small = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"])
+        sdp = mocatt.DeviceProblem(small, dev)
+        line["sweep_1M_g64"] = plain_timing(h, sdp, small, mocatt.default_opts(profile=1),
+                                            args.steps, flush, stream)
+        line["sweep_1M_g64"].update(workload="sweep_1M_g64", exp_mode="full")
+        del sdp
     if not args.no_forms and ws == 1:
-        line["forms"] = forms_section(h, dp, hp, sweep_s * 1e3)
+        line["forms"] = forms_section(h, dp, hp, statistics.mean(sweep_ms))
     if not args.no_tracks and ws == 1:
         line["tracks"] = tracks_section(h)
         line["transport"] = transport_section(h)
@@ -411,54 +499,126 @@ def _adjoint_vs_forward(h, dp, opts, fwd_ms, reps=3):
             "adjoint_ms": adj, "ratio": adj / fwd_ms}
 
 
-FORMS_ACCURACY = os.path.join(ROOT, "profiles", "forms_accuracy_gb300.json")
+# The precision forms and the workload they are graded and timed on: the wide-tau inputs
+# (sigT ~ logU(1e-3, 20), ds ~ U(1e-3, 2), tau over ~[1e-6, 40]) at 50M segments x 128
+# groups. Their accuracy is measured in the same run against the FP64 oracle (on the values
+# each form stores) on the first FORMS_SAMPLE_TRACKS tracks swept as a problem of their own;
+# tests/test_forms_gpu.py grades the whole workload.
+FORMS_WORKLOAD = "widetau_50M_g128"
+FORMS_SAMPLE_TRACKS = 10_000
+PRECISION_FORMS = {
+    "plain_fp32": ("MOC_PREC_FP32", "MOC_TALLY_ATOMIC_FP32"),
+    "fp32_stable": ("MOC_PREC_FP32_STABLE", "MOC_TALLY_ATOMIC_FP32"),
+    "fp32_stable_compensated": ("MOC_PREC_FP32_STABLE", "MOC_TALLY_COMPENSATED"),
+    "fp32_stable_fp64": ("MOC_PREC_FP32_STABLE", "MOC_TALLY_FP64"),
+    "bf16_stable": ("MOC_PREC_BF16", "MOC_TALLY_ATOMIC_FP32"),
+    "bf16_stable_compensated": ("MOC_PREC_BF16", "MOC_TALLY_COMPENSATED"),
+    "fp16_stable": ("MOC_PREC_FP16", "MOC_TALLY_ATOMIC_FP32"),
+}
+# The rule that picks chosen_form: normwise relative error <= 1e-5 for psi and for
+# fine_flux, against the FP64 oracle on the stored values.
+FORMS_TOL = 1e-5
+
+
+def _form_errors(hp, psi, ff, ref) -> dict:
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import parity
+
+    out = {}
+    G = hp.G
+    for name, x, r in (("psi", psi, ref["psi"]), ("fine_flux", ff, ref["ff"])):
+        mx, rms = parity.rel_err(x[:, :G], r[:, :G])
+        d = x[:, :G].astype(np.float64) - r[:, :G]
+        out[name] = {"max_rel": mx, "rms_rel": rms,
+                     "normwise": float(np.linalg.norm(d) / np.linalg.norm(r[:, :G]))}
+    return out
+
+
+def precision_section(h) -> dict:
+    """The precision forms on the wide-tau workload: every form timed on the full workload
+    (all passes, median of 3 after a warm-up), its error measured in this run on a track
+    sample against the FP64 oracle (test infrastructure, here only as the checker), and the
+    chosen form: the fastest non-plain form that meets the rule."""
+    import torch
+
+    import mocatt
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    w = mocatt.WORKLOADS[FORMS_WORKLOAD]
+    whp = mocatt.generate(w)
+    wdp = mocatt.DeviceProblem(whp)
+    units = float(whp.S) * whp.G
+    forms = {n: (getattr(mocatt, p), getattr(mocatt, t)) for n, (p, t) in PRECISION_FORMS.items()}
+    out = {"workload": FORMS_WORKLOAD, "segments": whp.S, "groups": whp.G, "tracks": whp.T,
+           "regions": whp.R}
+    times = {n: _time_fwd(h, wdp, mocatt.default_opts(profile=1, precision=p, tally=t))
+             for n, (p, t) in forms.items()}
+    del wdp
+    torch.cuda.empty_cache()
+
+    sub = whp.subset_tracks(range(min(FORMS_SAMPLE_TRACKS, whp.T)))
+    sdp = mocatt.DeviceProblem(sub)
+    psi0 = sdp.psi.clone()
+    results = {}
+    for n, (p, t) in forms.items():
+        sdp.psi.copy_(psi0)
+        sdp.fine_flux.zero_()
+        h.fwd(sdp, mocatt.default_opts(precision=p, tally=t))
+        if h.synchronize():
+            raise RuntimeError(f"device error in form {n}")
+        results[n] = (sdp.to_host("psi"), sdp.to_host("fine_flux"))
+    del sdp
+    threads = os.cpu_count() or 1
+    kind = {mocatt.MOC_PREC_FP32: mocatt.MOC_PREC_FP32_STABLE,
+            mocatt.MOC_PREC_FP32_STABLE: mocatt.MOC_PREC_FP32_STABLE,
+            mocatt.MOC_PREC_BF16: mocatt.MOC_PREC_BF16, mocatt.MOC_PREC_FP16: mocatt.MOC_PREC_FP16}
+    errors = {}
+    for storage in sorted(set(kind.values())):
+        qp, coef = oracle.quantized_inputs(sub, storage)
+        ref = oracle.fwd_fp64_coef(qp, coef, threads=threads)
+        for n, (p, _) in forms.items():
+            if kind[p] == storage:
+                errors[n] = _form_errors(sub, *results[n], ref)
+        del ref
+    t_plain = times["plain_fp32"]
+    precision = {}
+    for n in forms:
+        e = errors[n]
+        ok = e["psi"]["normwise"] <= FORMS_TOL and e["fine_flux"]["normwise"] <= FORMS_TOL
+        precision[n] = {"ms": times[n], "value": units / (times[n] * 1e-3),
+                        "speed_vs_plain": t_plain / times[n], "error": e, "meets_rule": ok}
+    ok = [n for n in precision if n != "plain_fp32" and precision[n]["meets_rule"]]
+    out["forms"] = precision
+    out["chosen_form"] = max(ok, key=lambda n: precision[n]["value"]) if ok else None
+    out["chosen_rule"] = ("normwise <= 1e-5: the fastest precision form whose psi and "
+                          "fine_flux normwise relative errors are <= 1e-5 against the FP64 "
+                          "oracle on the values it stores (RMS and maximum relative errors "
+                          "are reported beside them, not part of the rule)")
+    out["error_sample"] = (f"the first {sub.T} of {whp.T} tracks ({sub.S} segments x {sub.G} "
+                           f"groups) swept as a problem of their own, FP64 oracle on {threads} "
+                           f"host threads; the whole workload is graded by "
+                           f"tests/test_forms_gpu.py")
+    return out
 
 
 def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
-    """The three forms beside the plain sweep, timed on this GPU: the precision forms on the
-    bench workload (their accuracy against the FP64 oracle comes from the GPU test
-    tests/test_forms_gpu.py, recorded in profiles/forms_accuracy_gb300.json), the adjoint's
-    cost relative to one forward sweep, and the batching form against one launch per
-    problem."""
+    """The three forms beside the plain sweep, timed on this GPU: the precision forms on
+    their own wide-tau workload at full size, with their accuracy measured in this run
+    (precision_section), the adjoint's cost relative to one forward sweep, and the batching
+    form against one launch per problem."""
     import ctypes as C
 
     import torch
 
     import mocatt
 
-    out = {}
+    out = {"precision": precision_section(h)}
     plain = mocatt.default_opts(profile=1)
     t_plain = _time_fwd(h, dp, plain)
-    accuracy = {}
-    if os.path.exists(FORMS_ACCURACY):
-        with open(FORMS_ACCURACY) as f:
-            accuracy = json.load(f)
-    forms = {
-        "plain_fp32": (mocatt.MOC_PREC_FP32, mocatt.MOC_TALLY_ATOMIC_FP32),
-        "fp32_stable": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_ATOMIC_FP32),
-        "fp32_stable_compensated": (mocatt.MOC_PREC_FP32_STABLE, mocatt.MOC_TALLY_COMPENSATED),
-        "bf16_stable": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_ATOMIC_FP32),
-        "bf16_stable_compensated": (mocatt.MOC_PREC_BF16, mocatt.MOC_TALLY_COMPENSATED),
-        "fp16_stable": (mocatt.MOC_PREC_FP16, mocatt.MOC_TALLY_ATOMIC_FP32),
-    }
-    precision = {}
-    units = float(hp.S) * hp.G
-    for name, (prec, tally) in forms.items():
-        o = mocatt.default_opts(profile=1, precision=prec, tally=tally)
-        ms = t_plain if name == "plain_fp32" else _time_fwd(h, dp, o)
-        precision[name] = {"ms": ms, "value": units / (ms * 1e-3),
-                           "speed_vs_plain": t_plain / ms,
-                           "widetau_error": accuracy.get(name)}
-    ok = [n for n, v in precision.items() if n != "plain_fp32" and v["widetau_error"]
-          and v["widetau_error"]["psi"]["rms_rel"] <= 1e-5
-          and v["widetau_error"]["fine_flux"]["normwise"] <= 1e-5]
-    chosen = max(ok, key=lambda n: precision[n]["value"]) if ok else None
-    out["precision"] = precision
-    out["chosen_form"] = chosen
-    out["chosen_rule"] = ("fastest precision form whose psi RMS relative error is <= 1e-5 and "
-                          "whose fine_flux normwise error is <= 1e-5 against the FP64 oracle "
-                          "on the wide-tau inputs (tests/test_forms_gpu.py, recorded in "
-                          "profiles/forms_accuracy_gb300.json)")
 
     # adjoint: on the bench problem (50M x 128, the size the adjoint's cost target is
     # stated at) and on the gradient-check workload (5,000 lognormal tracks, ~2M
@@ -691,6 +851,8 @@ def main():
                     help="skip the track-generation line")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the precision / adjoint / batching measurements")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the table-mode and 1M x 64 lines")
     ap.add_argument("--segments", type=int, default=0,
                     help="override the workload's segment count (smaller profiling cases)")
     ap.add_argument("--tracks", type=int, default=0, help="override the track count")

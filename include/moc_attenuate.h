@@ -137,8 +137,7 @@ typedef struct {
                                      and return MOC_ERR_BAD_INDEX without touching
                                      fine_flux or psi                                     */
     int32_t vec;                  /* groups per lane: 0 = auto, else 1, 2 or 4          */
-    int32_t warps_per_block;      /* 0 = auto (8; 16 in table mode), else 1..16 (the
-                                     batching form: 1..8)                                 */
+    int32_t warps_per_block;      /* 0 = auto (8; 16 in table mode), else 1..16          */
     int32_t profile;              /* 1: time each kernel of the call with CUDA events on
                                      the call's stream (read with moc_last_timings)      */
     int32_t prefetch;             /* how far ahead of the arithmetic segments' cell blocks
@@ -203,12 +202,14 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *pr
 /*
  * Batching form: sweep several problems (different group counts, tracks of very uneven
  * length) in ONE persistent kernel launch. No single counterpart in the reference (its
- * run_kernel, src/cpu/kernel.c:3-73, sweeps one problem); each problem is swept exactly
- * as moc_attenuate_fwd with track_chunk = -1 would sweep it (plain form, either exp mode;
- * opts is shared; tracks are not cut into chunks).
- * Tracks are bucket-sorted by length on the device and consumed longest first from one
- * work queue; problems whose G does not fill a warp are swept by sub-warps carrying
- * several tracks each. The first call for a given set of problems (pointers and sizes)
+ * run_kernel, src/cpu/kernel.c:3-73, sweeps one problem); each problem is swept as
+ * moc_attenuate_fwd sweeps it (plain form, either exp mode; opts is shared). Long tracks
+ * are cut into chunks as opts.track_chunk says, with one chunk length for the whole
+ * batch (opts.track_chunk = 0: from the batch's total work; -1: never cut), so a problem's
+ * psi equals moc_attenuate_fwd's with that chunk length. Tracks (or chunk records) are
+ * bucket-sorted by length on the device and consumed longest first from one work queue;
+ * problems whose G does not fill a warp are swept by sub-warps carrying several tracks
+ * each. The first call for a given set of problems (pointers and sizes)
  * and options captures the whole sequence into a CUDA graph on the handle; later calls
  * with the same set replay it with one cudaGraphLaunch on `stream`. At most
  * MOC_BATCH_MAX_PROBLEMS problems, and at most 16 group ranges in total (a problem needs
@@ -222,24 +223,28 @@ moc_status_t moc_attenuate_fwd_batch(moc_handle_t handle, const moc_problem_t *p
                                      void *stream);
 
 /* Result of moc_autotune_batch. */
+#define MOC_TUNE_MAX_CANDIDATES 48
 typedef struct {
     int32_t vec;                  /* chosen groups per lane (1, 2 or 4)                  */
-    int32_t warps_per_block;      /* chosen warps per block (1, 2, 4 or 8)               */
-    int32_t tracks_per_block;     /* tracks a block carries at once for the first problem */
+    int32_t warps_per_block;      /* chosen warps per block (1..16)                      */
+    int32_t tracks_per_block;     /* tracks a block carries at once in a full-warp chunk
+                                     (one track per warp): warps_per_block                */
     float best_ms;                /* device time of one batched sweep with that choice   */
     int32_t n_candidates;
-    int32_t candidate_vec[16];
-    int32_t candidate_warps[16];
-    float candidate_ms[16];
+    int32_t candidate_vec[MOC_TUNE_MAX_CANDIDATES];
+    int32_t candidate_warps[MOC_TUNE_MAX_CANDIDATES];
+    float candidate_ms[MOC_TUNE_MAX_CANDIDATES];
 } moc_tune_result_t;
 
 /*
  * Autotuner of the batching form: times every (groups per lane in {1, 2, 4}) x
- * (warps per block in {1, 2, 4, 8}) on the given problems, keeps the fastest for this
- * set of problems in the handle (used by later moc_attenuate_fwd_batch calls whose opts
- * leave vec / warps_per_block at 0), and reports all candidates. psi and fine_flux of
- * the problems are saved before the trials and restored after them, so the call leaves
- * them unchanged. Synchronous.
+ * (tracks per block in {1, ..., 16}) on the given problems - a block of W warps carries W
+ * tracks at once in every full-warp group chunk (and 32/L times more in a remainder chunk
+ * swept by sub-warps of L lanes) - keeps the fastest for this set of problems in the
+ * handle (used by later moc_attenuate_fwd_batch calls whose opts leave vec /
+ * warps_per_block at 0), and reports all candidates. psi and fine_flux of the problems
+ * are saved before the trials and restored after them, so the call leaves them
+ * unchanged. Synchronous.
  */
 moc_status_t moc_autotune_batch(moc_handle_t handle, const moc_problem_t *problems,
                                 int32_t n_problems, const moc_fwd_opts_t *opts, void *stream,
@@ -272,8 +277,9 @@ moc_status_t moc_attenuate_adj(moc_handle_t handle, const moc_problem_t *problem
  * or a stateless call site with nowhere to keep a handle.
  *
  * Same sweep, same kernels and same results as moc_attenuate_fwd (plain form,
- * opts->precision = MOC_PREC_FP32, either exp mode; other precisions return
- * MOC_ERR_UNSUPPORTED), on the current CUDA device, asynchronous on `stream`. Its scratch is one fixed array in the library's
+ * opts->precision = MOC_PREC_FP32, either exp mode, opts->prefetch 0 or 1; other
+ * precisions and the bulk-copy ring return MOC_ERR_UNSUPPORTED), on the current CUDA
+ * device, asynchronous on `stream`. Its scratch is one fixed array in the library's
  * device image (every GPU that loads the library holds it, about 10.2 MiB, until the
  * process exits); nothing is allocated per call: no cudaMalloc, cudaFree or allocating
  * library routine. Limits: n_regions * n_intervals * group_stride <=

@@ -16,7 +16,7 @@
 //   dpsi'/ds = a0 D2/s^2 + a1 D1/s^3 + a2 dreuse/ds - psi p ds
 //   dreuse/ds = (2 tau - 2) tau/s + (2 tau p - 6 e)/s^4.
 // D1, D2 and D3 cancel for small tau (D3 ~ -tau^5/20 from tau^4 terms); below tau = 1
-// they come from their Taylor sums, like the forward's stable terms. The exponentials
+// they come from a fitted polynomial of their series, like the forward's stable terms. The exponentials
 // are recomputed from tau in the reverse sweep instead of being stored; psi entering
 // each segment is recorded by a first forward pass (one float per segment and group).
 //
@@ -45,21 +45,16 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
     AdjTerms r;
     if (tau < 2.0f) {
         // s4 = sum_{k>=4} (-1)^k tau^k / k! = tau^4 h, h = 1/24 - tau h5, with
-        // h5 = sum_{j>=0} (-tau)^j / (j+5)! (through tau^16: below 8e-10 of s4 at tau = 2)
-        // - the Horner chain's value one step before h. The threshold 2 keeps warps whose
-        // groups have tau up to 2 on this branch.
-        float h5 = 1.0f / 20922789888000.0f;       // 1/16!
-        h5 = fmaf(h5, -tau, 1.0f / 1307674368000.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 87178291200.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 6227020800.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 479001600.0f);  // 1/12!
-        h5 = fmaf(h5, -tau, 1.0f / 39916800.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 3628800.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 362880.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 40320.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 5040.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 720.0f);
-        h5 = fmaf(h5, -tau, 1.0f / 120.0f);
+        // h5 = sum_{j>=0} (-tau)^j / (j+5)!: a degree-5 polynomial fitted to the series on
+        // [0, 2] for least maximum relative error (weighted least squares on Chebyshev
+        // points, reweighted until the error equioscillates), within 1.3e-7 of h5 with FP32
+        // Horner steps, as the Taylor sum through tau^16 is. The threshold 2 keeps warps
+        // whose groups have tau up to 2 on this branch.
+        float h5 = fmaf(-1.626123236e-07f, tau, 2.524867341e-06f);
+        h5 = fmaf(h5, tau, -2.457161099e-05f);
+        h5 = fmaf(h5, tau, 1.983064285e-04f);
+        h5 = fmaf(h5, tau, -1.388870645e-03f);
+        h5 = fmaf(h5, tau, 8.333332837e-03f);
         const float h = fmaf(h5, -tau, 1.0f / 24.0f);
         const float t2 = tau * tau, t3 = t2 * tau, t4 = t2 * t2;
         const float s4 = h * t4;
@@ -92,7 +87,7 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
 // psi' of one segment, for the recording pass and the chunk maps: the forward sweep's
 // arithmetic (one ex2.approx for p, e = 1 - p). psi only needs the forward's FP32
 // accuracy, which the plain exponential meets; the cancelling derivative terms of the
-// reverse pass come from their Taylor sums (adj_terms). Also returns p and e/s.
+// reverse pass come from their series (adj_terms). Also returns p and e/s.
 template <int VEC>
 __device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VEC> &psi,
                                         Vec<VEC> &pv, Vec<VEC> &e1v)

@@ -1099,19 +1099,19 @@ moc_status_t moc_autotune_batch(moc_handle_t h, const moc_problem_t *probs, int3
     MOC_CUDA(h, cudaEventCreate(&b));
     std::memset(res, 0, sizeof(*res));
     res->best_ms = -1.0f;
-    const int vecs[3] = {1, 2, 4}, wpbs[4] = {1, 2, 4, 8};
+    const int vecs[3] = {1, 2, 4};
     for (int vi = 0; vi < 3 && s == MOC_OK; vi++)
-        for (int wi = 0; wi < 4 && s == MOC_OK; wi++) {
+        for (int w = 1; w <= 16 && s == MOC_OK; w++) {
             moc::BatchParams B;
             moc::BatchWork W;
             BatchSplit X;
             int blocks = 0;
-            if (build_batch(h, probs, n, o, vecs[vi], wpbs[wi], B, W, X, blocks)) continue;
+            if (build_batch(h, probs, n, o, vecs[vi], w, B, W, X, blocks)) continue;
             float best = 1e30f;
             for (int rep = 0; rep < 3 && s == MOC_OK; rep++) {
                 if ((s = copy_all(false))) break;
                 cudaEventRecord(a, st);
-                s = enqueue_batch(h, probs, n, o, B, W, X, vecs[vi], wpbs[wi], blocks, st);
+                s = enqueue_batch(h, probs, n, o, B, W, X, vecs[vi], w, blocks, st);
                 cudaEventRecord(b, st);
                 if (cudaEventSynchronize(b) != cudaSuccess) s = MOC_ERR_CUDA;
                 float ms = 0.0f;
@@ -1120,13 +1120,13 @@ moc_status_t moc_autotune_batch(moc_handle_t h, const moc_problem_t *probs, int3
             }
             const int c = res->n_candidates++;
             res->candidate_vec[c] = vecs[vi];
-            res->candidate_warps[c] = wpbs[wi];
+            res->candidate_warps[c] = w;
             res->candidate_ms[c] = best;
             if (res->best_ms < 0.0f || best < res->best_ms) {
                 res->best_ms = best;
                 res->vec = vecs[vi];
-                res->warps_per_block = wpbs[wi];
-                res->tracks_per_block = wpbs[wi] * (32 / B.sub[0].lpt);
+                res->warps_per_block = w;
+                res->tracks_per_block = w;
             }
         }
     const moc_status_t rs = copy_all(false);
@@ -1293,6 +1293,11 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     return MOC_OK;
 }
 
+// Pipelined host-buffer sweeps: the segments per part and the parts' relative sizes
+// (measured on GB300 at 50M x 128, 558 MB in and 77 MB out per call).
+constexpr int64_t PART_SEGMENTS = 8 << 20;
+constexpr double PART_WEIGHT[8] = {0.5, 1, 1, 1, 1, 1, 1, 1};
+
 moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
                                     const moc_fwd_opts_t *o)
 {
@@ -1310,11 +1315,12 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
                           p->sigT, p->source, p->fine_flux, p->psi};
     for (int k = 0; k < 8; k++)
         if ((s = ensure(h, &h->hbuf[k], &h->hcap[k], bytes[k] ? bytes[k] : 16))) return s;
-    // Large problems whose offsets partition [0, S] take the pipelined path (parts of
-    // about 8M segments, at most 8, measured best on GB300 at 50M x 128 against 2M and 4M;
-    // the first part is half the others, so the first sweep starts sooner); checked mode
-    // and smaller problems copy everything first.
-    const int parts = (int)std::min<int64_t>(8, std::max<int64_t>(1, S / (8 << 20)));
+    // Large problems whose offsets partition [0, S] take the pipelined path: parts of
+    // about PART_SEGMENTS segments (at most 8), sized by PART_WEIGHT (the first parts
+    // smaller, so the first sweep starts sooner, the last smaller, so less of the sweep
+    // remains when its copies start); checked mode and smaller problems copy everything
+    // first.
+    const int parts = (int)std::min<int64_t>(8, std::max<int64_t>(1, S / PART_SEGMENTS));
     if (!o->checked && parts > 1 && T >= parts) {
         bool csr = p->track_offsets[0] == 0 && p->track_offsets[T] == S;
         int64_t longest = 0;
@@ -1328,10 +1334,13 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
         if (csr) {
             int64_t cut[9];
             cut[0] = 0;
+            double wsum = 0.0;
+            for (int k = 0; k < parts; k++) wsum += PART_WEIGHT[k];
+            double acc = 0.0;
             for (int k = 1; k < parts; k++) {
-                // first track whose start reaches (k - 1/2)/(parts - 1/2) of the segments
-                const int64_t target =
-                    (int64_t)((double)S * (2.0 * k - 1.0) / (2.0 * parts - 1.0));
+                // first track whose start reaches the k-th cumulative share of the segments
+                acc += PART_WEIGHT[k - 1];
+                const int64_t target = (int64_t)((double)S * acc / wsum);
                 int64_t lo = cut[k - 1], hi = T;
                 while (lo < hi) {
                     const int64_t mid = (lo + hi) / 2;

@@ -148,7 +148,7 @@ __device__ __forceinline__ void attenuate_b(const float4 (&x)[VEC], float ds, fl
 
 // 7. the persistent sweep over the queue
 template <int VEC, int EK>
-__global__ void __launch_bounds__(256) batch_kernel(const BatchParams B, const int *perm,
+__global__ void __launch_bounds__(512) batch_kernel(const BatchParams B, const int *perm,
                                                     const int2 *queue)
 {
     extern __shared__ float2 s_tab[];
@@ -268,7 +268,7 @@ int batch_blocks_per_sm(int vec, int ek, int warps_per_block, size_t smem)
 {
     const void *fn = pick(vec, ek);
     int n = 0;
-    if (!fn || warps_per_block < 1 || warps_per_block > 8) return 0;
+    if (!fn || warps_per_block < 1 || warps_per_block > 16) return 0;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return 0;
@@ -282,7 +282,7 @@ cudaError_t launch_batch(const BatchParams &B, const BatchWork &W, int vec, int 
                          int warps_per_block, int blocks, cudaStream_t st)
 {
     const void *fn = pick(vec, ek);
-    if (!fn || blocks < 1 || warps_per_block < 1 || warps_per_block > 8)
+    if (!fn || blocks < 1 || warps_per_block < 1 || warps_per_block > 16)
         return cudaErrorInvalidValue;
     cudaError_t e;
     int64_t max_t = 0;

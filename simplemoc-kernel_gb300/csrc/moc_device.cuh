@@ -312,8 +312,7 @@ __device__ __forceinline__ float exp_neg_rr(float tau)
 // least squares on Chebyshev points, reweighted by the error until it equioscillates):
 // evaluated by FP32 Horner steps it is within 1.3e-7 of h, where the series itself
 // through tau^16 gives 9.3e-8, in 6 fused multiply-adds instead of 12. From tau = 2 on,
-// p comes from the range-reduced exponential and the cubic cancels at most ~5-fold. (The
-// threshold 2 keeps warps whose groups have tau up to 2 on one branch.)
+// p comes from the range-reduced exponential and the cubic cancels at most ~5-fold.
 constexpr float H6_0 = 4.166666791e-02f, H6_1 = -8.333321661e-03f, H6_2 = 1.388796256e-03f,
                 H6_3 = -1.981338719e-04f, H6_4 = 2.439518357e-05f, H6_5 = -2.442981440e-06f,
                 H6_6 = 1.485006180e-07f;
@@ -321,35 +320,51 @@ struct ExpTerms {
     float e, p, tme, cub;
 };
 
-__device__ __forceinline__ ExpTerms exp_terms_stable(float tau)
+// The four terms from the series, valid (and used) below tau = 2.
+__device__ __forceinline__ ExpTerms exp_terms_series(float tau)
 {
     ExpTerms r;
-    if (tau < 2.0f) {
-        float h = fmaf(H6_6, tau, H6_5);
-        h = fmaf(h, tau, H6_4);
-        h = fmaf(h, tau, H6_3);
-        h = fmaf(h, tau, H6_2);
-        h = fmaf(h, tau, H6_1);
-        h = fmaf(h, tau, H6_0);
-        const float t2 = tau * tau;
-        const float s4 = h * t2 * t2;
-        r.cub = 6.0f * s4;
-        r.tme = fmaf(t2, fmaf(tau, -1.0f / 6.0f, 0.5f), s4);
-        r.e = tau - r.tme;
-        r.p = 1.0f - r.e;
-    } else {
-        r.p = exp_neg_rr(tau);
-        r.e = 1.0f - r.p;
-        r.tme = tau - r.e;
-        r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
-    }
+    float h = fmaf(H6_6, tau, H6_5);
+    h = fmaf(h, tau, H6_4);
+    h = fmaf(h, tau, H6_3);
+    h = fmaf(h, tau, H6_2);
+    h = fmaf(h, tau, H6_1);
+    h = fmaf(h, tau, H6_0);
+    const float t2 = tau * tau;
+    const float s4 = h * t2 * t2;
+    r.cub = 6.0f * s4;
+    r.tme = fmaf(t2, fmaf(tau, -1.0f / 6.0f, 0.5f), s4);
+    r.e = tau - r.tme;
+    r.p = 1.0f - r.e;
+    return r;
+}
+
+// The four terms from the exponential, used from tau = 2 on.
+__device__ __forceinline__ ExpTerms exp_terms_direct(float tau)
+{
+    ExpTerms r;
+    r.p = exp_neg_rr(tau);
+    r.e = 1.0f - r.p;
+    r.tme = tau - r.e;
+    r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
+    return r;
+}
+
+// The series is evaluated for every tau (a warp whose groups straddle tau = 2 would run
+// both sides of a branch anyway); the exponential only where a lane has a group at
+// tau >= 2, and the larger tau take its terms. (Far above 2 the unused series overflows
+// to inf or NaN, which the selection drops.)
+__device__ __forceinline__ ExpTerms exp_terms_stable(float tau)
+{
+    ExpTerms r = exp_terms_series(tau);
+    if (tau >= 2.0f) r = exp_terms_direct(tau);
     return r;
 }
 
 // exp_terms_stable for two groups at once on the packed FP32 pipe: every packed operation
 // stands for the scalar one above in the same order (a - b and 1 - x as fma(b, -1, a) and
 // fma(x, -1, 1), which round once to the same value), so the terms are the scalar ones bit
-// for bit. A pair straddling tau = 2 takes the scalar form per group.
+// for bit.
 struct ExpTerms2 {
     float2 e, p, tme, cub;
 };
@@ -358,39 +373,41 @@ __device__ __forceinline__ ExpTerms2 exp_terms_stable2(float2 tau)
 {
     ExpTerms2 r;
     const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
-    const float2 mt = make_float2(-tau.x, -tau.y);
     auto c = [](float v) { return make_float2(v, v); };
-    if (tau.x < 2.0f && tau.y < 2.0f) {
-        float2 h = __ffma2_rn(c(H6_6), tau, c(H6_5));
-        h = __ffma2_rn(h, tau, c(H6_4));
-        h = __ffma2_rn(h, tau, c(H6_3));
-        h = __ffma2_rn(h, tau, c(H6_2));
-        h = __ffma2_rn(h, tau, c(H6_1));
-        h = __ffma2_rn(h, tau, c(H6_0));
-        const float2 t2 = __fmul2_rn(tau, tau);
-        const float2 s4 = __fmul2_rn(__fmul2_rn(h, t2), t2);
-        r.cub = __fmul2_rn(c(6.0f), s4);
-        r.tme = __ffma2_rn(t2, __ffma2_rn(tau, c(-1.0f / 6.0f), c(0.5f)), s4);
-        r.e = __ffma2_rn(r.tme, mone, tau);
-        r.p = __ffma2_rn(r.e, mone, one);
-    } else if (tau.x >= 2.0f && tau.y >= 2.0f) {
+    float2 h = __ffma2_rn(c(H6_6), tau, c(H6_5));
+    h = __ffma2_rn(h, tau, c(H6_4));
+    h = __ffma2_rn(h, tau, c(H6_3));
+    h = __ffma2_rn(h, tau, c(H6_2));
+    h = __ffma2_rn(h, tau, c(H6_1));
+    h = __ffma2_rn(h, tau, c(H6_0));
+    const float2 t2 = __fmul2_rn(tau, tau);
+    const float2 s4 = __fmul2_rn(__fmul2_rn(h, t2), t2);
+    r.cub = __fmul2_rn(c(6.0f), s4);
+    r.tme = __ffma2_rn(t2, __ffma2_rn(tau, c(-1.0f / 6.0f), c(0.5f)), s4);
+    r.e = __ffma2_rn(r.tme, mone, tau);
+    r.p = __ffma2_rn(r.e, mone, one);
+    const bool bx = tau.x >= 2.0f, by = tau.y >= 2.0f;
+    if (bx || by) {
         const float L2E_HI = 1.44269502162933349609375f, L2E_LO = 1.9259629911266175e-8f;
         const float LN2 = 0.693147180559945309f;
+        const float2 mt = make_float2(-tau.x, -tau.y);
         const float2 hi = __fmul2_rn(mt, c(L2E_HI));
         const float2 lo = __ffma2_rn(mt, c(L2E_LO),
                                      __ffma2_rn(mt, c(L2E_HI), make_float2(-hi.x, -hi.y)));
         const float2 q = make_float2(ex2_approx(hi.x), ex2_approx(hi.y));
-        r.p = __ffma2_rn(q, __fmul2_rn(lo, c(LN2)), q);
-        r.e = __ffma2_rn(r.p, mone, one);
-        r.tme = __ffma2_rn(r.e, mone, tau);
-        r.cub = __ffma2_rn(__fmul2_rn(tau, tau), __fadd2_rn(tau, c(-3.0f)),
-                           __fmul2_rn(c(6.0f), r.tme));
-    } else {
-        const ExpTerms u = exp_terms_stable(tau.x), w = exp_terms_stable(tau.y);
-        r.e = make_float2(u.e, w.e);
-        r.p = make_float2(u.p, w.p);
-        r.tme = make_float2(u.tme, w.tme);
-        r.cub = make_float2(u.cub, w.cub);
+        // each term replaces the series' where tau >= 2 as soon as it is formed
+        auto take = [bx, by](float2 &dst, float2 v) {
+            if (bx) dst.x = v.x;
+            if (by) dst.y = v.y;
+        };
+        const float2 p = __ffma2_rn(q, __fmul2_rn(lo, c(LN2)), q);
+        const float2 e = __ffma2_rn(p, mone, one);
+        const float2 tme = __ffma2_rn(e, mone, tau);
+        take(r.p, p);
+        take(r.e, e);
+        take(r.tme, tme);
+        take(r.cub, __ffma2_rn(__fmul2_rn(tau, tau), __fadd2_rn(tau, c(-3.0f)),
+                               __fmul2_rn(c(6.0f), tme)));
     }
     return r;
 }

@@ -11,6 +11,15 @@
 //   [3] FP32 FMA TFLOP/s         independent FMA chains, 2 flops each
 //   [4] MUFU ex2 Gop/s           ex2.approx chains
 //   [5] HBM read GB/s            float4 __ldcs over a 2 GiB buffer
+//   [6..8] row_mix: 512-byte rows, four streams per warp (gathers, reductions, 4:1 mix)
+//   [9] FP64 FMA TFLOP/s
+//   [10..12] row_mix_wide: the sweep's access shape at its most parallel: 1 KB rows read
+//       with one 256-bit load per lane (ld.global.nc.v8.f32) and 256-byte tally rows
+//       reduced with red.global.add.v2.f32, eight independent row streams per warp, the
+//       best of 8, 16 and 24 warps of 256 threads per SM: gathers only, reductions only,
+//       and the sweep's mix (a 1 KB gather per 256-byte reduction: per segment and group
+//       16 B read, 4 B reduced)
+//   [13] packed FP32 FMA TFLOP/s (fma.rn.f32x2 chains, 4 flops per instruction)
 // Every index is taken modulo its buffer; no kernel waits on anything.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -108,6 +117,69 @@ __global__ void row_mix(const float4 *__restrict__ rows, float *ff, int log2_row
         }
     }
     if (acc == 1234.5f) out[warp] = acc;
+}
+
+// The sweep's shape, as parallel as it can be issued: eight independent streams per warp,
+// each a random 1 KB row (64 float4; a lane reads float4 2l and 2l + 1 with one 256-bit
+// load) and a random 256-byte tally row (a lane reduces two floats).
+//   mode 0: gathers only; 1: reductions only; 2: one gather and one reduction per stream.
+constexpr int WIDE_K = 8;
+__global__ void row_mix_wide(const float4 *__restrict__ rows, float *ff, int log2_rows,
+                             int log2_ff_rows, int iters, int mode, float *out)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t st[WIDE_K];
+#pragma unroll
+    for (int k = 0; k < WIDE_K; k++) st[k] = hash32(warp * WIDE_K + k + 1);
+    const int sh = 32 - log2_rows, shf = 32 - log2_ff_rows;
+    float acc = 0.0f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < WIDE_K; k++) st[k] = st[k] * 1664525u + 1013904223u;
+        if (mode != 1) {
+            float v[WIDE_K][2];
+#pragma unroll
+            for (int k = 0; k < WIDE_K; k++) {
+                const float4 *p = rows + (size_t)(st[k] >> sh) * 64 + 2 * lane;
+                float a0, a1, a2, a3, a4, a5, a6, a7;
+                asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                             : "=f"(a0), "=f"(a1), "=f"(a2), "=f"(a3), "=f"(a4), "=f"(a5),
+                               "=f"(a6), "=f"(a7)
+                             : "l"(p));
+                v[k][0] = a0 + a5;
+                v[k][1] = a2 + a7;
+            }
+#pragma unroll
+            for (int k = 0; k < WIDE_K; k++) acc += v[k][0] * v[k][1];
+        }
+        if (mode != 0) {
+#pragma unroll
+            for (int k = 0; k < WIDE_K; k++) {
+                float *p = ff + (size_t)(st[k] >> shf) * 64 + 2 * lane;
+                asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(1.0f),
+                             "f"(1.0f)
+                             : "memory");
+            }
+        }
+    }
+    if (acc == 1234.5f) out[warp] = acc;
+}
+
+__global__ void fma2_chains(float *out, int iters, float a, float b)
+{
+    float2 x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = make_float2(threadIdx.x + k, threadIdx.x - k);
+    const float2 aa = make_float2(a, a), bb = make_float2(b, b);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = __ffma2_rn(x[k], aa, bb);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k].x + x[k].y;
+    if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 __global__ void fma_chains(float *out, int iters, float a, float b)
@@ -231,6 +303,32 @@ extern "C" int mocpeak_run(double *res, int n_res)
         res[7] = warps * it * 2 * 512.0 / (ms * 1e-3) / 1e9;
         ms = time_ms([&] { row_mix<<<blocks, threads>>>((const float4 *)rows, ff, lr, lf, it, 2, out); }, 5);
         res[8] = warps * it * 5 * 512.0 / (ms * 1e-3) / 1e9;
+    }
+
+    if (n_res >= 14) {
+        // 2^16 rows of 1 KB (64 MiB: the sweep's half of its cell blocks) to gather from,
+        // 2^16 tally rows of 256 B (16 MiB) to reduce into
+        const int lr = 16, lf = 16, it = 400;
+        double best[3] = {0.0, 0.0, 0.0};
+        for (int per_sm : {8, 16, 24}) {
+            int can = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&can, row_mix_wide, threads, 0);
+            if (can * (threads / 32) < per_sm) continue;
+            const int b = sms * per_sm / (threads / 32);
+            const double warps = (double)b * (threads / 32);
+            const double bytes[3] = {1024.0, 256.0, 1280.0};
+            for (int mode = 0; mode < 3; mode++) {
+                ms = time_ms([&] { row_mix_wide<<<b, threads>>>((const float4 *)rows, ff, lr, lf, it, mode, out); }, 5);
+                const double gbs = warps * it * WIDE_K * bytes[mode] / (ms * 1e-3) / 1e9;
+                if (gbs > best[mode]) best[mode] = gbs;
+            }
+        }
+        res[10] = best[0];
+        res[11] = best[1];
+        res[12] = best[2];
+        const int fiters = 10000;
+        ms = time_ms([&] { fma2_chains<<<blocks, threads>>>(out, fiters, 0.999f, 1e-3f); }, 5);
+        res[13] = (double)blocks * threads * fiters * 8 * 4.0 / (ms * 1e-3) / 1e12;
     }
 
     const cudaError_t e = cudaDeviceSynchronize();

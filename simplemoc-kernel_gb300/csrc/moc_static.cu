@@ -87,6 +87,9 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     moc_status_t s = moc::check_args(p, o);
     if (s) return s;
     if (o->precision != MOC_PREC_FP32) return MOC_ERR_UNSUPPORTED;  // the plain form only
+    // the register loops only: the bulk-copy ring's bounded waits report a timeout through
+    // an error word, which this entry point has no handle to return to the caller
+    if (o->prefetch > 1) return MOC_ERR_UNSUPPORTED;
     const int64_t cell_groups = (int64_t)p->n_regions * p->n_intervals * p->group_stride;
     if (cell_groups > MOC_NOALLOC_MAX_CELL_GROUPS) return MOC_ERR_TOO_LARGE;
     if (o->exp_mode == MOC_EXP_TABLE && o->table_points > MOC_NOALLOC_MAX_TABLE_POINTS)
@@ -149,8 +152,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
     cfg.exp_kind = o->exp_mode == MOC_EXP_TABLE ? moc::EXPK_TABLE : moc::EXPK_PLAIN;
     cfg.warps_per_block =
         o->warps_per_block ? o->warps_per_block : moc::auto_warps_per_block(cfg.exp_kind);
-    cfg.prefetch = o->prefetch > 1 ? o->prefetch : 1;
-    if (moc::fwd_bulk(cfg) && cfg.vec > 1 && !moc::f32_pairs(cfg.vec)) return MOC_ERR_UNSUPPORTED;
+    cfg.prefetch = 1;
     const int per_sm = moc::fwd_blocks_per_sm(cfg, o->table_points);
     if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
     cfg.blocks = per_sm * sms;
@@ -161,7 +163,7 @@ extern "C" moc_status_t moc_attenuate_fwd_noalloc(const moc_problem_t *p,
 
     NA_CUDA(moc::launch_prep_block(p->sigT, p->source, blk, p->n_regions, p->n_intervals,
                                    p->group_stride, o->dz, o->zin, o->mu, o->mu2, st, false,
-                                   moc::f32_pairs(cfg.vec), moc::fwd_bulk(cfg) ? cfg.vec : 0));
+                                   moc::f32_pairs(cfg.vec)));
     NA_CUDA(moc::launch_fwd(sp, cfg, st));
     return MOC_OK;
 }

@@ -79,8 +79,8 @@ class MocTimings(C.Structure):
 class MocTuneResult(C.Structure):
     _fields_ = [("vec", C.c_int32), ("warps_per_block", C.c_int32),
                 ("tracks_per_block", C.c_int32), ("best_ms", C.c_float),
-                ("n_candidates", C.c_int32), ("candidate_vec", C.c_int32 * 16),
-                ("candidate_warps", C.c_int32 * 16), ("candidate_ms", C.c_float * 16)]
+                ("n_candidates", C.c_int32), ("candidate_vec", C.c_int32 * 48),
+                ("candidate_warps", C.c_int32 * 48), ("candidate_ms", C.c_float * 48)]
 
 
 class MocGeometry(C.Structure):

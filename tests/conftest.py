@@ -9,7 +9,10 @@ for p in (os.path.join(ROOT, "simplemoc-kernel_gb300"), os.path.join(ROOT, "orac
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REFERENCE_SOURCES = "/root/reference"
+# The reference's sources, where mounted (MOC_REFERENCE_SOURCES, else a "reference"
+# directory beside this repository): the live pin tests build against them.
+REFERENCE_SOURCES = os.environ.get("MOC_REFERENCE_SOURCES") or os.path.join(
+    os.path.dirname(ROOT), "reference")
 
 
 def pytest_configure(config):

@@ -83,4 +83,8 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference's sources: the argument, MOC_REFERENCE_SOURCES, or a "reference"
+    # directory beside this repository
+    default = os.environ.get("MOC_REFERENCE_SOURCES") or os.path.join(
+        os.path.dirname(ROOT), "reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else default)

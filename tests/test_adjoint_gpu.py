@@ -68,9 +68,11 @@ def test_adjoint_vs_fp64_cpu_adjoint(handle, adj_problem, adj_ref, chunk):
     out = {k: rel(a[:, :G], ref[r][:, :G]) for k, a, r in (
         ("sigT", ds, "d_sigT"), ("source", dsrc, "d_source"), ("psi_in", dpsi, "d_psi_in"))}
     print(out)
+    # measured on GB300: max 1.9e-4 - 2.2e-4 (sigT), 4.2e-4 - 6.1e-4 (source), 4.7e-4
+    # (psi_in); RMS 1.7e-6 - 2.3e-6 for every output and chunk length
     for k, (mx, rms) in out.items():
-        assert rms <= 1e-4, (k, mx, rms)
-        assert mx <= 1e-2, (k, mx, rms)
+        assert rms <= 1e-5, (k, mx, rms)
+        assert mx <= 2e-3, (k, mx, rms)
 
 
 def test_adjoint_split_keeps_whole_tracks_bitwise(handle, adj_problem):

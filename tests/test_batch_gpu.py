@@ -92,8 +92,9 @@ def test_autotuner_reports_and_restores(handle):
     opts = mocatt.default_opts()
     handle.check(mocatt.lib().moc_autotune_batch(handle.ptr, arr, 3, C.byref(opts), None,
                                                  C.byref(res)))
-    assert res.n_candidates == 12
-    assert res.vec in (1, 2, 4) and res.warps_per_block in (1, 2, 4, 8)
+    assert res.n_candidates == 48  # groups per lane {1, 2, 4} x tracks per block 1..16
+    assert res.vec in (1, 2, 4) and 1 <= res.warps_per_block <= 16
+    assert res.tracks_per_block == res.warps_per_block
     assert res.best_ms == min(res.candidate_ms[:res.n_candidates])
     print({(res.candidate_vec[k], res.candidate_warps[k]): round(res.candidate_ms[k], 3)
            for k in range(res.n_candidates)}, "tracks/block", res.tracks_per_block)
