@@ -157,6 +157,11 @@ def cpu_baseline(workload, sample_tracks: int, steps: int, warmup: int,
     return r
 
 
+# Roofline peaks measured by this process (run_peaks after the timed steps); they take
+# precedence over the committed profiles/peaks_gb300.json.
+IN_RUN_PEAKS: dict = {}
+
+
 def load_peaks() -> dict:
     peaks = {}
     if os.path.exists(MEASURED_PEAKS):
@@ -170,6 +175,10 @@ def load_peaks() -> dict:
     if os.path.exists(PEAKS_FILE):
         with open(PEAKS_FILE) as f:
             peaks.update(json.load(f))
+        peaks["peaks_measured"] = "by bench.py --peaks (profiles/peaks_gb300.json)"
+    if IN_RUN_PEAKS:
+        peaks.update(IN_RUN_PEAKS)
+        peaks["peaks_measured"] = "in this run (csrc/moc_peaks.cu after the timed steps)"
     return peaks
 
 
@@ -269,9 +278,9 @@ def sweep_roofline(hp, sweep_ms: float, prep_ms: float, split_ms: float) -> dict
     if mixes:
         key = max(mixes, key=mixes.get)
         roof["peak"] = mixes[key]
-        roof["peak_source"] = (f"profiles/peaks_gb300.json {key} (bench.py --peaks, "
-                               f"csrc/moc_peaks.cu), measured {peaks.get('date', 'undated')}"
-                               f" at SM clock {peaks.get('clocks', {}).get('sm_mhz')} MHz")
+        roof["peak_source"] = (f"{key}, measured {peaks.get('peaks_measured')} on "
+                               f"{peaks.get('date', 'an undated run')} at SM clock "
+                               f"{peaks.get('clocks', {}).get('sm_mhz')} MHz")
         roof["frac"] = roof["achieved"] / roof["peak"]
         roof["frac_layout"] = roof["achieved_layout"] / roof["peak"]
         terms["l2"] = survey_b * units / (roof["peak"] * 1e9) * 1e3
@@ -422,7 +431,13 @@ def gpu_arm(args, workload):
             torch.distributed.destroy_process_group()
         return
 
-    # ---- roofline of the sweep kernel ----------------------------------------------
+    # ---- roofline of the sweep kernel, against peaks measured now --------------------
+    if not args.no_peaks_run:
+        try:
+            IN_RUN_PEAKS.update(run_peaks())
+        except (OSError, RuntimeError) as e:
+            print(f"warning: roofline microbenchmarks failed ({e}); using the committed "
+                  f"peaks", file=sys.stderr)
     roof = sweep_roofline(hp, statistics.mean(sweep_ms), statistics.mean(prep_ms),
                           statistics.mean(split_ms))
 
@@ -853,6 +868,9 @@ def main():
                     help="skip the precision / adjoint / batching measurements")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the table-mode and 1M x 64 lines")
+    ap.add_argument("--no-peaks-run", action="store_true",
+                    help="take the roofline peaks from profiles/peaks_gb300.json instead "
+                         "of measuring them after the timed steps")
     ap.add_argument("--segments", type=int, default=0,
                     help="override the workload's segment count (smaller profiling cases)")
     ap.add_argument("--tracks", type=int, default=0, help="override the track count")
