@@ -342,36 +342,42 @@ def _fnv64_words(payload: bytes) -> int:
     return h
 
 
-def trackfile_bytes(R, I, off, reg, itv, ds, cells=None) -> bytes:
+def trackfile_bytes(R, I, off, reg, itv, ds, cells=None, compact=False) -> bytes:
     """A track file's bytes from the header's layout; cells overrides region * I +
-    interval (to make files with bad indices and a valid checksum)."""
+    interval (to make files with bad indices and a valid checksum). compact: version 2,
+    lengths as IEEE half (numpy's float16 conversion, round to nearest even)."""
     import struct
 
     off = np.ascontiguousarray(off, "<i8")
     if cells is None:
         cells = np.asarray(reg, np.uint64) * I + np.asarray(itv, np.uint64)
-    payload = (off.tobytes() + np.ascontiguousarray(cells, "<u4").tobytes() +
-               np.ascontiguousarray(ds, "<f4").tobytes())
-    head = TRACKFILE_MAGIC + struct.pack("<IIqqiiQ", 1, 48, len(off) - 1, len(ds), R, I,
-                                         _fnv64_words(payload))
+    lengths = (np.ascontiguousarray(ds, np.float32).astype("<f2") if compact else
+               np.ascontiguousarray(ds, "<f4"))
+    payload = off.tobytes() + np.ascontiguousarray(cells, "<u4").tobytes() + lengths.tobytes()
+    head = TRACKFILE_MAGIC + struct.pack("<IIqqiiQ", 2 if compact else 1, 48, len(off) - 1,
+                                         len(ds), R, I, _fnv64_words(payload))
     return head + payload
 
 
 def trackfile_parse(data: bytes):
-    """(R, I, offsets, region, interval, ds) of a track file's bytes; ValueError if the
-    header, the length or the checksum is wrong."""
+    """(R, I, offsets, region, interval, ds) of a track file's bytes (either version; half
+    lengths widened to float32); ValueError if the header, the length or the checksum is
+    wrong."""
     import struct
 
     if len(data) < 48 or data[:8] != TRACKFILE_MAGIC:
         raise ValueError("not a track file")
     version, hbytes, T, S, R, I, cs = struct.unpack("<IIqqiiQ", data[8:48])
-    if version != 1 or hbytes != 48 or len(data) != 48 + 8 * (T + 1) + 8 * S:
+    per = {1: 8, 2: 6}.get(version)
+    if per is None or hbytes != 48 or len(data) != 48 + 8 * (T + 1) + per * S:
         raise ValueError("bad header or length")
     payload = data[48:]
     if _fnv64_words(payload) != cs:
         raise ValueError("checksum")
     off = np.frombuffer(payload, "<i8", T + 1)
     cells = np.frombuffer(payload, "<u4", S, 8 * (T + 1))
-    ds = np.frombuffer(payload, "<f4", S, 8 * (T + 1) + 4 * S)
-    return R, I, off.copy(), (cells // I).astype(np.int32), (cells % I).astype(np.uint8), ds.copy()
-
+    if version == 1:
+        ds = np.frombuffer(payload, "<f4", S, 8 * (T + 1) + 4 * S).copy()
+    else:
+        ds = np.frombuffer(payload, "<f2", S, 8 * (T + 1) + 4 * S).astype(np.float32)
+    return R, I, off.copy(), (cells // I).astype(np.int32), (cells % I).astype(np.uint8), ds

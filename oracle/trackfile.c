@@ -5,11 +5,23 @@
  * the same segment files as the GPU program (mocatt_run -f). Restated from the header's
  * layout, independently of the library's reader (simplemoc-kernel_gb300/host/trackfile.c).
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "oracle.h"
+
+/* IEEE half -> float, exact: 5-bit exponent (bias 15), 10-bit fraction, subnormals in
+ * units of 2^-24. */
+static float half_to_float(uint16_t h)
+{
+    const int e = (h >> 10) & 31, m = h & 1023;
+    const float sign = (h & 0x8000) ? -1.0f : 1.0f;
+    if (e == 0) return sign * ldexpf((float)m, -24);
+    if (e == 31) return m ? NAN : sign * INFINITY;
+    return sign * ldexpf((float)(1024 + m), e - 25);
+}
 
 static uint64_t fnv_update(uint64_t h, const uint8_t *p, size_t n, uint8_t *carry, int *nc)
 {
@@ -47,11 +59,12 @@ int oracle_trackfile_read(const char *path, int64_t *T_out, int64_t *S_out, int3
     memcpy(&R, h + 32, 4);
     memcpy(&I, h + 36, 4);
     memcpy(&sum, h + 40, 8);
-    if (version != 1 || hbytes != 48 || T < 0 || S < 0 || R < 1 || I < 1) {
+    if ((version != 1 && version != 2) || hbytes != 48 || T < 0 || S < 0 || R < 1 || I < 1) {
         fclose(f);
         return -1;
     }
-    const size_t n = (size_t)(8 * (T + 1) + 8 * S);
+    const int per = version == 1 ? 8 : 6;  /* bytes per segment: cell + length */
+    const size_t n = (size_t)(8 * (T + 1) + per * S);
     uint8_t *payload = (uint8_t *)malloc(n ? n : 1);
     if (!payload || fread(payload, 1, n, f) != n || fgetc(f) != EOF) {
         free(payload);
@@ -84,7 +97,12 @@ int oracle_trackfile_read(const char *path, int64_t *T_out, int64_t *S_out, int3
             (*reg)[j] = (int32_t)(c / (uint32_t)I);
             (*itv)[j] = (uint8_t)(c % (uint32_t)I);
         }
-        if (ok) memcpy(*ds, payload + 8 * (T + 1) + 4 * S, (size_t)S * 4);
+        if (ok && version == 1) memcpy(*ds, payload + 8 * (T + 1) + 4 * S, (size_t)S * 4);
+        for (int64_t j = 0; ok && version == 2 && j < S; j++) {
+            uint16_t hv;
+            memcpy(&hv, payload + 8 * (T + 1) + 4 * S + 2 * j, 2);
+            (*ds)[j] = half_to_float(hv);
+        }
     }
     free(payload);
     if (!ok) {

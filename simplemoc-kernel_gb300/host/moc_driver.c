@@ -18,6 +18,7 @@
  *                tracks, regions and intervals replace -s, -k and -r; the tables and psi
  *                stay seeded)
  *   -w file      write the generated segments to a track file before sweeping
+ *   -W file      the same in the compact version (half lengths, 6 bytes per segment)
  * -t is accepted for command-line compatibility and ignored (the sweep runs on the GPU).
  */
 #include "moc_attenuate.h"
@@ -48,6 +49,7 @@ static void usage(void)
            "  -n <repeats>        Sweeps to time\n"
            "  -f <file>           Sweep the segments of a track file\n"
            "  -w <file>           Write the generated segments to a track file\n"
+           "  -W <file>           Same, compact (half lengths, 6 bytes per segment)\n"
            "  -t <threads>        Accepted and ignored\n");
 }
 
@@ -68,6 +70,7 @@ int main(int argc, char **argv)
     long tracks = -1;
     int intervals = 5;
     const char *in_file = NULL, *out_file = NULL;
+    int compact = 0;
     for (int i = 1; i < argc; i++) {
         const char *a = argv[i];
         const int more = i + 1 < argc;
@@ -81,6 +84,10 @@ int main(int argc, char **argv)
         else if (!strcmp(a, "-x")) table = 1;
         else if (!strcmp(a, "-f") && more) in_file = argv[++i];
         else if (!strcmp(a, "-w") && more) out_file = argv[++i];
+        else if (!strcmp(a, "-W") && more) {
+            out_file = argv[++i];
+            compact = 1;
+        }
         else {
             usage();
             return 1;
@@ -131,8 +138,11 @@ int main(int argc, char **argv)
         moc_synth_fill(&spec, off, psi, sigT, source, reg, itv, ds);
     }
     if (out_file) {
-        const moc_status_t fs = moc_trackfile_write(out_file, tracks, segments, regions,
-                                                    intervals, off, reg, itv, ds);
+        const moc_status_t fs =
+            compact ? moc_trackfile_write_compact(out_file, tracks, segments, regions,
+                                                  intervals, off, reg, itv, ds)
+                    : moc_trackfile_write(out_file, tracks, segments, regions, intervals, off,
+                                          reg, itv, ds);
         if (fs != MOC_OK) {
             fprintf(stderr, "%s: %s\n", out_file, moc_status_string(fs));
             return 1;

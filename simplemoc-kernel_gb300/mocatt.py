@@ -114,7 +114,8 @@ class MocEigenOpts(C.Structure):
 class MocTrackfileInfo(C.Structure):
     """moc_trackfile_info_t (include/moc_trackfile.h)."""
     _fields_ = [("n_tracks", C.c_int64), ("n_segments", C.c_int64), ("n_regions", C.c_int32),
-                ("n_intervals", C.c_int32), ("checksum", C.c_uint64)]
+                ("n_intervals", C.c_int32), ("checksum", C.c_uint64), ("version", C.c_int32),
+                ("bytes_per_segment", C.c_int32)]
 
 
 # moc_track_t as a numpy record (112 bytes)
@@ -168,6 +169,8 @@ ABI = {
                                      _P, _P, _P]),
     "moc_trackfile_write": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
                                       _P, _P, _P, _P]),
+    "moc_trackfile_write_compact": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_int32,
+                                              C.c_int32, _P, _P, _P, _P]),
     "moc_trackfile_info": (C.c_int, [C.c_char_p, C.POINTER(MocTrackfileInfo)]),
     "moc_trackfile_read": (C.c_int, [C.c_char_p, _P, _P, _P, _P]),
     "moc_region_sigT": (C.c_int, [_P, C.POINTER(MocXS), _P, C.c_int32, _P, _P]),
@@ -526,15 +529,16 @@ def geometry_materials(g) -> np.ndarray:
     return np.where(ring == g.n_rings, 0, 1 + ring).astype(np.int32)
 
 
-def write_trackfile(path: str, R: int, I: int, off, reg, itv, ds) -> None:
-    """moc_trackfile_write of CSR descriptors (host arrays)."""
+def write_trackfile(path: str, R: int, I: int, off, reg, itv, ds, compact: bool = False) -> None:
+    """moc_trackfile_write (or, compact, moc_trackfile_write_compact: half lengths) of CSR
+    descriptors (host arrays)."""
     off = np.ascontiguousarray(off, np.int64)
     reg = np.ascontiguousarray(reg, np.int32)
     itv = np.ascontiguousarray(itv, np.uint8)
     ds = np.ascontiguousarray(ds, np.float32)
-    st = lib().moc_trackfile_write(os.fsencode(path), len(off) - 1, len(reg), R, I,
-                                   off.ctypes.data, reg.ctypes.data, itv.ctypes.data,
-                                   ds.ctypes.data)
+    fn = lib().moc_trackfile_write_compact if compact else lib().moc_trackfile_write
+    st = fn(os.fsencode(path), len(off) - 1, len(reg), R, I, off.ctypes.data, reg.ctypes.data,
+            itv.ctypes.data, ds.ctypes.data)
     if st:
         raise MocError(st)
 

@@ -88,7 +88,8 @@ def test_corrupt_and_inconsistent_files(tmp_path):
         "truncated": good[:-5],
         "trailing bytes": good + b"x",
         "bad magic": b"MOCTRK02" + good[8:],
-        "bad version": good[:8] + (2).to_bytes(4, "little") + good[12:],
+        "bad version": good[:8] + (3).to_bytes(4, "little") + good[12:],
+        "version 2 header on a version 1 payload": good[:8] + (2).to_bytes(4, "little") + good[12:],
         "header only": good[:48],
     }
     R, I, off, reg, itv, ds = golden_arrays()
@@ -153,3 +154,68 @@ def test_gpu_program_writes_without_a_device(tmp_path):
     np.testing.assert_array_equal(off, hp.track_offsets)
     np.testing.assert_array_equal(reg, hp.seg_region)
     assert ds.tobytes() == hp.seg_ds.tobytes()
+
+
+def test_compact_version_matches_the_oracle_and_rounds_lengths_to_half(tmp_path):
+    """Version 2 (6 bytes per segment): the library's bytes equal the oracle's own writer
+    (numpy's float16 rounding), and reading widens the half lengths exactly."""
+    R, I, off, reg, itv, ds = golden_arrays()
+    p = str(tmp_path / "c.moctrk")
+    mocatt.write_trackfile(p, R, I, off, reg, itv, ds, compact=True)
+    data = open(p, "rb").read()
+    assert data == oracle.trackfile_bytes(R, I, off, reg, itv, ds, compact=True)
+    S = len(ds)
+    assert len(data) == 48 + 8 * len(off) + 6 * S
+    gR, gI, goff, greg, gitv, gds = mocatt.read_trackfile(p)
+    assert (gR, gI) == (R, I)
+    np.testing.assert_array_equal(goff, off)
+    np.testing.assert_array_equal(greg, reg)
+    np.testing.assert_array_equal(gitv, itv)
+    half = ds.astype(np.float16).astype(np.float32)
+    assert gds.tobytes() == half.tobytes()
+    assert np.all(np.abs(gds - ds) <= 2.0 ** -11 * np.abs(ds) + 2.0 ** -25)
+    info = mocatt.MocTrackfileInfo()
+    assert mocatt.lib().moc_trackfile_info(os.fsencode(p), mocatt.C.byref(info)) == 0
+    assert (info.version, info.bytes_per_segment) == (2, 6)
+    # the oracle's parser and the CPU harness read it too
+    assert oracle.trackfile_parse(data)[5].tobytes() == half.tobytes()
+    exe = os.path.join(oracle.HERE, "_build", "cpu_bench")
+    out = subprocess.run([exe, "--groups", "8", "--track-file", p, "--steps", "1",
+                          "--warmup", "0", "--threads", "2"], capture_output=True, text=True,
+                         timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert json.loads(out.stdout.strip().splitlines()[-1])["sample_segments"] == S
+
+
+def test_half_rounding_edge_cases(tmp_path):
+    """Ties to even, subnormal halves, the largest finite half; lengths that would not be
+    finite halves (or are negative or NaN) are refused."""
+    vals = np.array([0.0, 1.0, 1.0 + 2.0 ** -11, 1.0 + 3 * 2.0 ** -11, 2.0 ** -24, 2.0 ** -25,
+                     3 * 2.0 ** -26, 6.0e-5, 1e-7, 65504.0, 65519.0, 0.7, 1.0 / 3.0],
+                    np.float32)
+    S = len(vals)
+    off = np.array([0, S], np.int64)
+    reg = np.zeros(S, np.int32)
+    itv = np.zeros(S, np.uint8)
+    p = str(tmp_path / "e.moctrk")
+    mocatt.write_trackfile(p, 1, 2, off, reg, itv, vals, compact=True)
+    assert open(p, "rb").read() == oracle.trackfile_bytes(1, 2, off, reg, itv, vals, compact=True)
+    got = mocatt.read_trackfile(p)[5]
+    assert got.tobytes() == vals.astype(np.float16).astype(np.float32).tobytes()
+    for bad in (65520.0, -1.0, np.nan, np.inf):
+        with pytest.raises(mocatt.MocError) as e:
+            mocatt.write_trackfile(p, 1, 2, np.array([0, 1], np.int64), reg[:1], itv[:1],
+                                   np.array([bad], np.float32), compact=True)
+        assert e.value.status == mocatt.MOC_ERR_INVALID_ARG
+
+
+def test_gpu_program_writes_compact_files_without_a_device(tmp_path):
+    exe = os.path.join(mocatt.BUILD, "mocatt_run")
+    p = str(tmp_path / "gen.moctrk")
+    subprocess.run([exe, "-s", "3000", "-e", "8", "-r", "40", "-k", "7", "-W", p],
+                   capture_output=True, text=True, timeout=120)
+    R, I, off, reg, itv, ds = mocatt.read_trackfile(p)
+    hp = mocatt.generate(mocatt.Workload("driver", 1, 40, 5, 8, 7, 3000))
+    np.testing.assert_array_equal(reg, hp.seg_region)
+    assert ds.tobytes() == hp.seg_ds.astype(np.float16).astype(np.float32).tobytes()
+    assert os.path.getsize(p) == 48 + 8 * 8 + 6 * 3000
