@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 struct moc_handle_s {
@@ -1293,6 +1294,52 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     return MOC_OK;
 }
 
+// The device address of `bytes` bytes of page-locked host memory at p mapped into the
+// current device's address space (pinned memory under unified addressing), or null for any
+// other array. Its first and its last byte must both map, at the same offset, so an array
+// whose allocation is shorter than its stated size is never read in place.
+const void *mapped_on_device(const void *p, size_t bytes)
+{
+    if (!p || bytes == 0) return nullptr;
+    const void *ends[2] = {p, static_cast<const char *>(p) + (bytes - 1)};
+    const char *dev[2] = {nullptr, nullptr};
+    for (int k = 0; k < 2; k++) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, ends[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+        dev[k] = static_cast<const char *>(a.devicePointer);
+    }
+    return dev[1] - dev[0] == (ptrdiff_t)(bytes - 1) ? dev[0] : nullptr;
+}
+
+// The host-buffer sweep on arrays the GPU reads in place (NVLink-C2C on Grace-Blackwell,
+// PCIe elsewhere): descriptors, offsets, psi and the tables stay in the caller's pinned
+// memory; psi is updated there; only the tallies live on the device (the caller's
+// fine_flux copied up, the sweep's reductions added into it, copied back), since
+// reductions into host memory would cross the link once per segment and group.
+moc_status_t fwd_host_mapped(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
+                             const moc_problem_t &mp)
+{
+    moc_status_t s;
+    const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
+    const size_t ff_bytes = (size_t)ncell * p->group_stride * 4;
+    if ((s = ensure(h, &h->hbuf[6], &h->hcap[6], ff_bytes ? ff_bytes : 16))) return s;
+    cudaStream_t st = h->hstream;
+    moc_problem_t d = mp;
+    d.fine_flux = static_cast<float *>(h->hbuf[6]);
+    MOC_CUDA(h, cudaMemcpyAsync(d.fine_flux, p->fine_flux, ff_bytes, cudaMemcpyHostToDevice, st));
+    MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));
+    if ((s = fwd_device(h, &d, o, st))) return s;
+    MOC_CUDA(h, cudaMemcpyAsync(p->fine_flux, d.fine_flux, ff_bytes, cudaMemcpyDeviceToHost, st));
+    MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));  // reported here
+    MOC_CUDA(h, cudaStreamSynchronize(st));
+    return *h->err_host ? MOC_ERR_BAD_INDEX : MOC_OK;
+}
+
 // Pipelined host-buffer sweeps: the segments per part and the parts' relative sizes
 // (measured on GB300 at 50M x 128, 558 MB in and 77 MB out per call).
 constexpr int64_t PART_SEGMENTS = 8 << 20;
@@ -1307,6 +1354,26 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
     if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
     const int64_t T = p->n_tracks, S = p->n_segments, Gs = p->group_stride;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
+    // Page-locked, mapped arrays (cudaHostAlloc / cudaHostRegister, e.g. torch's
+    // pin_memory): the sweep reads them in place (fwd_host_mapped). Checked mode, empty
+    // problems and any array that is not mapped take the copies below.
+    if (!o->checked && S > 0 && T > 0) {
+        moc_problem_t mp = *p;
+        bool all = true;
+        auto map = [&](const void *q, size_t n, auto *&out) {
+            const void *dq = mapped_on_device(q, n);
+            all = all && dq;
+            out = static_cast<std::remove_reference_t<decltype(out)>>(const_cast<void *>(dq));
+        };
+        map(p->track_offsets, (size_t)(T + 1) * 8, mp.track_offsets);
+        map(p->seg_region, (size_t)S * 4, mp.seg_region);
+        map(p->seg_interval, (size_t)S, mp.seg_interval);
+        map(p->seg_ds, (size_t)S * 4, mp.seg_ds);
+        map(p->sigT, (size_t)p->n_regions * Gs * 4, mp.sigT);
+        map(p->source, (size_t)ncell * Gs * 4, mp.source);
+        map(p->psi, (size_t)T * Gs * 4, mp.psi);
+        if (all) return fwd_host_mapped(h, p, o, mp);
+    }
     const size_t bytes[8] = {
         (size_t)(T + 1) * 8, (size_t)S * 4, (size_t)S, (size_t)S * 4,
         (size_t)p->n_regions * Gs * 4, (size_t)ncell * Gs * 4, (size_t)ncell * Gs * 4,

@@ -159,6 +159,44 @@ def test_pipelined_host_entry_point(handle, name, kw):
     assert handle.synchronize() == 0
 
 
+def pinned_copy(hp):
+    """hp with every array in page-locked host memory (torch's pin_memory: mapped into the
+    device's address space under unified addressing)."""
+    import torch
+
+    q = hp.copy()
+    keep = []
+    for name in mocatt.DeviceProblem.NAMES:
+        t = torch.from_numpy(np.ascontiguousarray(getattr(hp, name))).pin_memory()
+        keep.append(t)
+        setattr(q, name, t.numpy())
+    return q, keep
+
+
+@pytest.mark.parametrize("name,kw", [
+    ("sweep_1M_g64", dict(regions=120, tracks=48, segments=12_000)),
+    ("sweep_50M_g128", dict(segments=18_000_000, tracks=40_000, regions=2_000, groups=64)),
+    ("adjoint_2M_g64", dict(tracks=50_000)),
+])
+def test_host_entry_point_reads_pinned_arrays_in_place(handle, name, kw):
+    """Pinned host arrays are swept in place (descriptors, offsets, tables and psi read and
+    psi written over the host link, the tallies on the device): psi equals the device entry
+    point's bit for bit, both outputs are inside the FP64 tolerance, and a bad segment is
+    still reported."""
+    hp = mocatt.generate(mocatt.WORKLOADS[name].with_(**kw))
+    psi_d, ff_d = run_gpu(handle, hp)
+    q, keep = pinned_copy(hp)
+    handle.fwd_host(q)
+    assert np.array_equal(q.psi, psi_d)
+    ref = oracle.fwd_fp64(hp)
+    parity.check_plain(q.psi, q.fine_flux, ref, hp.G)
+    b, keep_b = pinned_copy(hp)
+    b.seg_region[hp.S - 3] = hp.R + 1
+    with pytest.raises(mocatt.MocError):
+        handle.fwd_host(b)
+    assert handle.synchronize() == 0
+
+
 def test_bad_index_is_skipped_and_reported(handle):
     """A segment with an out-of-range region is skipped by the kernel's own bounds check
     and reported; checked mode rejects the problem before touching anything."""
@@ -235,3 +273,25 @@ def test_sweep_50M_g128_full_size(handle, exp_mode):
     sub_opts.track_chunk = -1
     p_sub, _ = run_gpu(handle, sub, sub_opts)
     assert np.array_equal(p_sub, psi[sample])
+
+
+def test_arrays_of_another_device_are_refused():
+    """A sweep on one device refuses arrays that live on another (it may have no peer
+    access to them): MOC_ERR_INVALID_ARG from the handle and the no-allocation entry
+    points. Needs two GPUs."""
+    import ctypes as C
+
+    import torch
+
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    hp = small(regions=20, tracks=4, segments=100)
+    dp1 = mocatt.DeviceProblem(hp, "cuda:1")
+    h0 = mocatt.Handle(0)
+    o = mocatt.default_opts()
+    st = mocatt.lib().moc_attenuate_fwd(h0.ptr, C.byref(dp1.c_struct()), C.byref(o), None)
+    assert st == mocatt.MOC_ERR_INVALID_ARG
+    h0.close()
+    torch.cuda.set_device(0)
+    st = mocatt.lib().moc_attenuate_fwd_noalloc(C.byref(dp1.c_struct()), C.byref(o), None)
+    assert st == mocatt.MOC_ERR_INVALID_ARG
