@@ -190,6 +190,28 @@ moc_status_t moc_attenuate_fwd(moc_handle_t handle, const moc_problem_t *problem
                                const moc_fwd_opts_t *opts, void *stream);
 
 /*
+ * Compact segment descriptors: 6 bytes per segment instead of 9 (the on-disk compact track
+ * format's payload, include/moc_trackfile.h). No counterpart in the reference, whose
+ * segments are random draws (src/cpu/kernel.c:47-50).
+ */
+typedef struct {
+    const uint32_t *seg_cell;     /* [S] region * n_intervals + interval, < R * I        */
+    const uint16_t *seg_ds_half;  /* [S] segment length as IEEE half bits (>= 0)         */
+} moc_compact_segments_t;
+
+/*
+ * moc_attenuate_fwd on compact descriptors: the problem's seg_region, seg_interval and
+ * seg_ds are not used (they may be NULL); every segment's cell and half length come from
+ * `segments` (device memory, 4- and 2-byte aligned). The sweep widens each length to FP32
+ * exactly, so its results are moc_attenuate_fwd's on those widened lengths. Every form,
+ * exp mode and option of moc_attenuate_fwd applies; cells out of range are skipped and
+ * reported as there (or refused up front with opts->checked).
+ */
+moc_status_t moc_attenuate_fwd_compact(moc_handle_t handle, const moc_problem_t *problem,
+                                       const moc_compact_segments_t *segments,
+                                       const moc_fwd_opts_t *opts, void *stream);
+
+/*
  * Same sweep, with every pointer of `problem` in HOST memory: the call copies the
  * inputs to device memory held by the handle, sweeps, copies psi and fine_flux back,
  * and returns when the host arrays hold the results. This is the drop-in for a host

@@ -317,9 +317,12 @@ moc_status_t pick_config(moc_handle_t h, const moc_problem_t *p, const moc_fwd_o
 
 // The forward sweep of one problem on device buffers. prep = false: the cell blocks of
 // this problem's tables are already in h->blk (a later part of a pipelined call).
+// compact: the segments as 32-bit cells and half lengths (moc_attenuate_fwd_compact) in
+// place of the problem's three descriptor arrays.
 moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
                         cudaStream_t st, bool prep = true,
-                        unsigned long long *counter = nullptr)
+                        unsigned long long *counter = nullptr,
+                        const moc_compact_segments_t *compact = nullptr)
 {
     // queue heads: [0] the sweep's, [1] the map pass's (a pipelined call gives every other
     // part its own pair so that parts on two streams can overlap)
@@ -342,6 +345,10 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
     sp.reg = p->seg_region;
     sp.itv = p->seg_interval;
     sp.ds = p->seg_ds;
+    if (compact) {
+        sp.cell = compact->seg_cell;
+        sp.ds16 = compact->seg_ds_half;
+    }
     sp.blk = h->blk;
     sp.ff = p->fine_flux;
     sp.psi = p->psi;
@@ -995,6 +1002,30 @@ moc_status_t moc_attenuate_fwd(moc_handle_t h, const moc_problem_t *p,
     for (const void *q : ptrs)
         if (!device_accessible(q, h->device)) return MOC_ERR_INVALID_ARG;
     return fwd_device(h, p, o, static_cast<cudaStream_t>(stream));
+}
+
+moc_status_t moc_attenuate_fwd_compact(moc_handle_t h, const moc_problem_t *p,
+                                       const moc_compact_segments_t *c,
+                                       const moc_fwd_opts_t *o, void *stream)
+{
+    if (!h || !p || !c) return MOC_ERR_INVALID_ARG;
+    if (p->n_segments > 0 && (!c->seg_cell || !c->seg_ds_half)) return MOC_ERR_INVALID_ARG;
+    if (!aligned(c->seg_cell, 4) || !aligned(c->seg_ds_half, 2)) return MOC_ERR_MISALIGNED;
+    if ((int64_t)p->n_regions * p->n_intervals > (int64_t)UINT32_MAX) return MOC_ERR_INVALID_ARG;
+    // the problem's own descriptor arrays are not used: check the rest with them standing
+    // for the compact ones
+    moc_problem_t q = *p;
+    q.seg_region = reinterpret_cast<const int32_t *>(c->seg_cell);
+    q.seg_interval = reinterpret_cast<const uint8_t *>(c->seg_cell);
+    q.seg_ds = reinterpret_cast<const float *>(c->seg_cell);
+    moc_status_t s = check_problem(&q, o);
+    if (s) return s;
+    if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
+    const void *ptrs[] = {p->track_offsets, c->seg_cell, c->seg_ds_half, p->sigT, p->source,
+                          p->fine_flux, p->psi};
+    for (const void *x : ptrs)
+        if (!device_accessible(x, h->device)) return MOC_ERR_INVALID_ARG;
+    return fwd_device(h, &q, o, static_cast<cudaStream_t>(stream), true, nullptr, c);
 }
 
 moc_status_t moc_attenuate_fwd_batch(moc_handle_t h, const moc_problem_t *probs, int32_t n,

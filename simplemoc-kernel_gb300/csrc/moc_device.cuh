@@ -284,23 +284,6 @@ __device__ __forceinline__ float ex2_approx(float x)
     return r;
 }
 
-// exp(-tau) for tau >= 0 with a Cody-Waite split of the argument (Cody & Waite, 1980):
-// x = -tau * log2(e) is formed as hi + lo, where hi is the rounded product and lo the
-// rounding error of that product plus the tail of log2(e); 2^x = 2^hi * (1 + lo ln 2).
-// The split removes the error of rounding x, which grows with |x|; what is left is the
-// error of ex2.approx itself.
-__device__ __forceinline__ float exp_neg_rr(float tau)
-{
-    const float L2E_HI = 1.44269502162933349609375f;     // float nearest log2(e)
-    const float L2E_LO = 1.9259629911266175e-8f;         // log2(e) - L2E_HI
-    const float LN2 = 0.693147180559945309f;
-    const float hi = -tau * L2E_HI;
-    // the rounding error of hi, then the tail of log2(e), each in one fused step
-    const float lo = fmaf(-tau, L2E_LO, fmaf(-tau, L2E_HI, -hi));
-    const float p = ex2_approx(hi);
-    return fmaf(p, lo * LN2, p);
-}
-
 // The exponential terms of the attenuation, accurate for every tau >= 0:
 //   e = 1 - exp(-tau), p = exp(-tau), tme = tau - e,
 //   cub = tau(tau(tau-3)+6) - 6e.
@@ -312,7 +295,9 @@ __device__ __forceinline__ float exp_neg_rr(float tau)
 // least squares on Chebyshev points, reweighted by the error until it equioscillates):
 // evaluated by FP32 Horner steps it is within 1.3e-7 of h, where the series itself
 // through tau^16 gives 9.3e-8, in 6 fused multiply-adds instead of 12. From tau = 2 on,
-// p comes from the range-reduced exponential and the cubic cancels at most ~5-fold.
+// p = ex2.approx(-tau log2 e): rounding the argument costs p a relative error of about
+// tau 2^-24 (2.4e-6 at tau = 40, where p is 4e-18), and p <= e^-2 there, so e = 1 - p,
+// tme = tau - e and the cubic (which cancels at most ~5-fold) keep FP32 accuracy.
 constexpr float H6_0 = 4.166666791e-02f, H6_1 = -8.333321661e-03f, H6_2 = 1.388796256e-03f,
                 H6_3 = -1.981338719e-04f, H6_4 = 2.439518357e-05f, H6_5 = -2.442981440e-06f,
                 H6_6 = 1.485006180e-07f;
@@ -343,7 +328,7 @@ __device__ __forceinline__ ExpTerms exp_terms_series(float tau)
 __device__ __forceinline__ ExpTerms exp_terms_direct(float tau)
 {
     ExpTerms r;
-    r.p = exp_neg_rr(tau);
+    r.p = ex2_approx(tau * -1.44269504088896341f);
     r.e = 1.0f - r.p;
     r.tme = tau - r.e;
     r.cub = fmaf(tau * tau, tau - 3.0f, 6.0f * r.tme);
@@ -388,19 +373,13 @@ __device__ __forceinline__ ExpTerms2 exp_terms_stable2(float2 tau)
     r.p = __ffma2_rn(r.e, mone, one);
     const bool bx = tau.x >= 2.0f, by = tau.y >= 2.0f;
     if (bx || by) {
-        const float L2E_HI = 1.44269502162933349609375f, L2E_LO = 1.9259629911266175e-8f;
-        const float LN2 = 0.693147180559945309f;
-        const float2 mt = make_float2(-tau.x, -tau.y);
-        const float2 hi = __fmul2_rn(mt, c(L2E_HI));
-        const float2 lo = __ffma2_rn(mt, c(L2E_LO),
-                                     __ffma2_rn(mt, c(L2E_HI), make_float2(-hi.x, -hi.y)));
-        const float2 q = make_float2(ex2_approx(hi.x), ex2_approx(hi.y));
+        const float2 m = __fmul2_rn(tau, c(-1.44269504088896341f));
+        const float2 p = make_float2(ex2_approx(m.x), ex2_approx(m.y));
         // each term replaces the series' where tau >= 2 as soon as it is formed
         auto take = [bx, by](float2 &dst, float2 v) {
             if (bx) dst.x = v.x;
             if (by) dst.y = v.y;
         };
-        const float2 p = __ffma2_rn(q, __fmul2_rn(lo, c(LN2)), q);
         const float2 e = __ffma2_rn(p, mone, one);
         const float2 tme = __ffma2_rn(e, mone, tau);
         take(r.p, p);

@@ -86,6 +86,10 @@ struct SweepParams {
     const int32_t *reg;
     const uint8_t *itv;
     const float *ds;
+    // compact descriptors (moc_attenuate_fwd_compact), in place of reg / itv / ds when
+    // cell is set: cell = region * I + interval, ds as IEEE half bits
+    const uint32_t *cell;
+    const uint16_t *ds16;
     const void *blk;     // [R*I][Gs]: (sigT, q0, q1*mu, q2*mu2) per cell and group,
                          // float4 or four 16-bit values (StoreKind)
     float *ff;           // [R*I][Gs]

@@ -224,17 +224,30 @@ __device__ __forceinline__ void attenuate(const Blk<VEC> &x, float ds, float wei
     attenuate_row<VEC, EK, f32_pairs(VEC)>(x.v, ds, weight, tr, psi, tally, pmul);
 }
 
-// Lane-parallel descriptor decode of segment j: its cell index and its ds. Out-of-range
-// regions or intervals are reported through the error word. A segment past the item's
-// end or with an out-of-range index decodes to cell `none`
-// with ds = 0: -1 (skipped by the loops that test it), or the null cell R*I, whose block
-// (sigT 1, coefficients 0) makes the segment an exact no-op (p = 1, every term 0).
+// Lane-parallel descriptor decode of segment j: its cell index and its ds, from the three
+// arrays or from the compact pair (a 32-bit cell index and a half length; the branch is
+// the same for every lane and taken once per 32-segment window). Out-of-range regions,
+// intervals or cells are reported through the error word. A segment past the item's end
+// or with an out-of-range index decodes to cell `none` with ds = 0: -1 (skipped by the
+// loops that test it), or the null cell R*I, whose block (sigT 1, coefficients 0) makes
+// the segment an exact no-op (p = 1, every term 0).
 __device__ __forceinline__ void decode(const SweepParams &P, int64_t j, int64_t end, int none,
                                        int &cell, float &ds)
 {
     cell = none;
     ds = 0.0f;
     if (j < end) {
+        if (P.cell) {
+            const uint32_t c = ld_stream(P.cell + j);
+            const unsigned short hb = ld_stream(reinterpret_cast<const unsigned short *>(P.ds16) + j);
+            if (c < (uint32_t)P.R * (uint32_t)P.I) {
+                cell = (int)c;
+                ds = __half2float(__ushort_as_half(hb));
+            } else {
+                atomicOr(P.err, DEVERR_INDEX);
+            }
+            return;
+        }
         const int r = ld_stream(P.reg + j);
         const int iv = ld_stream(P.itv + j);
         const float d = ld_stream(P.ds + j);
@@ -661,7 +674,8 @@ __global__ void check_kernel(const SweepParams P)
     }
     if (tid == 0 && (P.off[0] != 0 || P.off[P.T] != P.S)) bad |= DEVERR_OFFSETS;
     for (int64_t j = tid; j < P.S; j += stride) {
-        if ((unsigned)P.reg[j] >= (unsigned)P.R || (unsigned)P.itv[j] >= (unsigned)P.I)
+        if (P.cell ? P.cell[j] >= (uint32_t)P.R * (uint32_t)P.I
+                   : ((unsigned)P.reg[j] >= (unsigned)P.R || (unsigned)P.itv[j] >= (unsigned)P.I))
             bad |= DEVERR_INDEX;
     }
     if (bad) atomicOr(P.err, bad);

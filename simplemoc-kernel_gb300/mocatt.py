@@ -71,6 +71,11 @@ class MocFwdOpts(C.Structure):
     ]
 
 
+class MocCompactSegments(C.Structure):
+    """moc_compact_segments_t (include/moc_attenuate.h)."""
+    _fields_ = [("seg_cell", C.c_void_p), ("seg_ds_half", C.c_void_p)]
+
+
 class MocTimings(C.Structure):
     _fields_ = [("prep_ms", C.c_float), ("sweep_ms", C.c_float), ("finish_ms", C.c_float),
                 ("launches", C.c_int32), ("split_ms", C.c_float)]
@@ -143,6 +148,9 @@ ABI = {
     "moc_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
     "moc_destroy": (C.c_int, [_P]),
     "moc_attenuate_fwd": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts), _P]),
+    "moc_attenuate_fwd_compact": (C.c_int, [_P, C.POINTER(MocProblem),
+                                            C.POINTER(MocCompactSegments),
+                                            C.POINTER(MocFwdOpts), _P]),
     "moc_attenuate_fwd_host": (C.c_int, [_P, C.POINTER(MocProblem), C.POINTER(MocFwdOpts)]),
     "moc_synchronize": (C.c_int, [_P, _P]),
     "moc_build_exp_table": (C.c_int, [C.c_int32, C.c_float, _P, C.POINTER(C.c_float),
@@ -659,6 +667,19 @@ class Handle:
         prob = dp.c_struct()
         self.check(lib().moc_attenuate_fwd(self._h, C.byref(prob), C.byref(opts),
                                            C.c_void_p(s.cuda_stream)))
+
+    def fwd_compact(self, dp: DeviceProblem, cell, ds_half, opts: MocFwdOpts | None = None,
+                    stream=None):
+        """moc_attenuate_fwd_compact: dp's tables, offsets, psi and fine_flux with the
+        segments given as device tensors of 32-bit cells (region * I + interval) and half
+        lengths (int16/uint16 bit patterns or float16)."""
+        import torch
+        opts = opts or default_opts()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        prob = dp.c_struct()
+        segs = MocCompactSegments(cell.data_ptr(), ds_half.data_ptr())
+        self.check(lib().moc_attenuate_fwd_compact(self._h, C.byref(prob), C.byref(segs),
+                                                   C.byref(opts), C.c_void_p(s.cuda_stream)))
 
     def adj(self, dp: DeviceProblem, w, v, opts: MocFwdOpts | None = None, stream=None):
         """moc_attenuate_adj: gradients of L = sum w . fine_flux_out + sum v . psi_out with

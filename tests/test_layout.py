@@ -31,6 +31,7 @@ STRUCTS = {
     "moc_xs_t": mocatt.MocXS,
     "moc_eigen_opts_t": mocatt.MocEigenOpts,
     "moc_trackfile_info_t": mocatt.MocTrackfileInfo,
+    "moc_compact_segments_t": mocatt.MocCompactSegments,
 }
 # C type name -> the numpy record dtype that mirrors it
 RECORDS = {"moc_track_t": mocatt.TRACK_DTYPE}
