@@ -75,6 +75,12 @@ def hbm_compulsory_bytes(hp) -> float:
             + 2 * 16.0 * R * I * Gs + 2 * 4.0 * R * I * Gs)
 
 
+# --precision: the form the timed steps sweep (the headline is the plain FP32 form; the
+# others exist for profiling a precision form on the same harness)
+PRECISION_ARG = {"fp32": "MOC_PREC_FP32", "fp32_stable": "MOC_PREC_FP32_STABLE",
+                 "bf16": "MOC_PREC_BF16", "fp16": "MOC_PREC_FP16"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -237,7 +243,9 @@ def reference_arm(args, workload):
 def config_of(args, w) -> dict:
     return {"workload": w.name, "segments": w.segments, "groups": w.groups,
             "tracks": w.tracks, "regions": w.regions, "intervals": w.intervals,
-            "exp_mode": args.exp, "form": "plain FP32 (reference computation, drop-in)",
+            "exp_mode": args.exp,
+            "form": ("plain FP32 (reference computation, drop-in)" if args.precision == "fp32"
+                     else f"precision form {args.precision} (FP32 tallies)"),
             "l2": "flushed between steps (256 MiB write); 0.5 GB of descriptors per step "
                   "exceeds L2", "parallelism": "replicas only (one sweep per GPU)"}
 
@@ -357,7 +365,7 @@ def gpu_arm(args, workload):
     hp = mocatt.generate(workload)
     dp = mocatt.DeviceProblem(hp, dev)
     h = mocatt.Handle(local)
-    kw = dict(profile=1)
+    kw = dict(profile=1, precision=getattr(mocatt, PRECISION_ARG[args.precision]))
     if args.exp == "table":
         kw.update(exp_mode=mocatt.MOC_EXP_TABLE, table_points=args.table_points, table_max=10.0)
     opts = mocatt.default_opts(**kw)
@@ -455,7 +463,7 @@ def gpu_arm(args, workload):
         "config": config_of(args, workload), "roofline": roof, "e2e": e2e,
         "gpu_launches": launches, "clocks": clk,
     }
-    if ws == 1 and args.exp == "full" and not args.no_extra:
+    if ws == 1 and args.exp == "full" and args.precision == "fp32" and not args.no_extra:
         # the other plain-form lines: the table exp mode on this workload, and the
         # reference's CPU-sized problem (1M segments x 64 groups)
         line["table"] = plain_timing(h, dp, hp, mocatt.default_opts(
@@ -863,6 +871,8 @@ def main():
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--workload", default="sweep_50M_g128")
     ap.add_argument("--exp", default="full", choices=["full", "table"])
+    ap.add_argument("--precision", default="fp32", choices=sorted(PRECISION_ARG),
+                    help="the form the timed steps sweep (default: the plain FP32 form)")
     ap.add_argument("--table-points", type=int, default=10_000)
     ap.add_argument("--cpu-sample-tracks", type=int, default=20_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
