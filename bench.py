@@ -12,8 +12,8 @@ no dataset; it draws random inputs itself).
                (256 MiB write) between steps
   e2e          the same metric through moc_attenuate_fwd_host on page-locked host
                arrays: every step moves all inputs in and psi + fine_flux out over the
-               host link (the sweep reads the mapped arrays in place; the tallies are
-               copied both ways)
+               host link (the sweep reads the mapped descriptors and psi in place, the
+               tables are copied up, the tallies are added into fine_flux in place)
   roofline     the sweep kernel against its binding resource (L2: row gathers +
                tally reductions), with the HBM fraction beside it
   cpu_baseline the reference sweep restated in C (OpenMP over tracks, per-cell locks,
@@ -435,9 +435,11 @@ def gpu_arm(args, workload):
         e2e = {"value": ws * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                "call": "moc_attenuate_fwd_host on page-locked host arrays, returns synced: "
-                       "the arrays are mapped, so the sweep reads descriptors, offsets, "
-                       "tables and psi in place over the host link and writes psi back "
-                       "there; fine_flux is copied up and back around the sweep"}
+                       "the arrays are mapped, so the sweep reads descriptors, offsets "
+                       "and psi in place over the host link and writes psi back there; "
+                       "sigT and source are copied up first; the tallies start at zero "
+                       "on the device and a last pass adds them into the mapped "
+                       "fine_flux in place"}
 
     if rank != 0:
         if ws > 1:

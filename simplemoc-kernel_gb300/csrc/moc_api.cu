@@ -1347,24 +1347,42 @@ const void *mapped_on_device(const void *p, size_t bytes)
 }
 
 // The host-buffer sweep on arrays the GPU reads in place (NVLink-C2C on Grace-Blackwell,
-// PCIe elsewhere): descriptors, offsets, psi and the tables stay in the caller's pinned
-// memory; psi is updated there; only the tallies live on the device (the caller's
-// fine_flux copied up, the sweep's reductions added into it, copied back), since
-// reductions into host memory would cross the link once per segment and group.
+// PCIe elsewhere): descriptors, offsets and psi stay in the caller's pinned memory and psi
+// is updated there. The tables (read a few times each by the cell-block pass) are copied
+// up first. The tallies live on the device, since reductions into host memory would cross
+// the link once per segment and group: they start at zero, and a last pass adds them to
+// the caller's fine_flux in place when that is mapped too (else fine_flux is copied up
+// before the sweep and back after it).
 moc_status_t fwd_host_mapped(moc_handle_t h, const moc_problem_t *p, const moc_fwd_opts_t *o,
                              const moc_problem_t &mp)
 {
     moc_status_t s;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
     const size_t ff_bytes = (size_t)ncell * p->group_stride * 4;
-    if ((s = ensure(h, &h->hbuf[6], &h->hcap[6], ff_bytes ? ff_bytes : 16))) return s;
+    const size_t sig_bytes = (size_t)p->n_regions * p->group_stride * 4;
+    if ((s = ensure(h, &h->hbuf[4], &h->hcap[4], sig_bytes)) ||
+        (s = ensure(h, &h->hbuf[5], &h->hcap[5], ff_bytes)) ||
+        (s = ensure(h, &h->hbuf[6], &h->hcap[6], ff_bytes)))
+        return s;
     cudaStream_t st = h->hstream;
     moc_problem_t d = mp;
+    d.sigT = static_cast<const float *>(h->hbuf[4]);
+    d.source = static_cast<const float *>(h->hbuf[5]);
     d.fine_flux = static_cast<float *>(h->hbuf[6]);
-    MOC_CUDA(h, cudaMemcpyAsync(d.fine_flux, p->fine_flux, ff_bytes, cudaMemcpyHostToDevice, st));
+    float *ff_mapped = static_cast<float *>(const_cast<void *>(mapped_on_device(p->fine_flux, ff_bytes)));
+    MOC_CUDA(h, cudaMemcpyAsync(h->hbuf[4], p->sigT, sig_bytes, cudaMemcpyHostToDevice, st));
+    MOC_CUDA(h, cudaMemcpyAsync(h->hbuf[5], p->source, ff_bytes, cudaMemcpyHostToDevice, st));
+    if (ff_mapped)
+        MOC_CUDA(h, cudaMemsetAsync(d.fine_flux, 0, ff_bytes, st));
+    else
+        MOC_CUDA(h, cudaMemcpyAsync(d.fine_flux, p->fine_flux, ff_bytes, cudaMemcpyHostToDevice, st));
     MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));
     if ((s = fwd_device(h, &d, o, st))) return s;
-    MOC_CUDA(h, cudaMemcpyAsync(p->fine_flux, d.fine_flux, ff_bytes, cudaMemcpyDeviceToHost, st));
+    if (ff_mapped)  // fine_flux += tallies, in the caller's memory
+        MOC_CUDA(h, moc::launch_finish(ff_mapped, d.fine_flux, nullptr,
+                                       ncell * p->group_stride, st));
+    else
+        MOC_CUDA(h, cudaMemcpyAsync(p->fine_flux, d.fine_flux, ff_bytes, cudaMemcpyDeviceToHost, st));
     MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));  // reported here
     MOC_CUDA(h, cudaStreamSynchronize(st));
@@ -1385,9 +1403,9 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
     if (cudaSetDevice(h->device) != cudaSuccess) return MOC_ERR_NO_DEVICE;
     const int64_t T = p->n_tracks, S = p->n_segments, Gs = p->group_stride;
     const int64_t ncell = (int64_t)p->n_regions * p->n_intervals;
-    // Page-locked, mapped arrays (cudaHostAlloc / cudaHostRegister, e.g. torch's
-    // pin_memory): the sweep reads them in place (fwd_host_mapped). Checked mode, empty
-    // problems and any array that is not mapped take the copies below.
+    // Page-locked, mapped descriptors, offsets and psi (cudaHostAlloc / cudaHostRegister,
+    // e.g. torch's pin_memory): the sweep reads them in place (fwd_host_mapped). Checked
+    // mode, empty problems and arrays that are not mapped take the copies below.
     if (!o->checked && S > 0 && T > 0) {
         moc_problem_t mp = *p;
         bool all = true;
@@ -1400,8 +1418,6 @@ moc_status_t moc_attenuate_fwd_host(moc_handle_t h, const moc_problem_t *p,
         map(p->seg_region, (size_t)S * 4, mp.seg_region);
         map(p->seg_interval, (size_t)S, mp.seg_interval);
         map(p->seg_ds, (size_t)S * 4, mp.seg_ds);
-        map(p->sigT, (size_t)p->n_regions * Gs * 4, mp.sigT);
-        map(p->source, (size_t)ncell * Gs * 4, mp.source);
         map(p->psi, (size_t)T * Gs * 4, mp.psi);
         if (all) return fwd_host_mapped(h, p, o, mp);
     }
