@@ -15,7 +15,7 @@
 //   dFI/ds   = a0 D1/s^3 + psi D2/s^2 + a1 dreuse/ds + a2 D3/(3 s^5)
 //   dpsi'/ds = a0 D2/s^2 + a1 D1/s^3 + a2 dreuse/ds - psi p ds
 //   dreuse/ds = (2 tau - 2) tau/s + (2 tau p - 6 e)/s^4.
-// D1, D2 and D3 cancel for small tau (D3 ~ -tau^5/20 from tau^4 terms); below tau = 1
+// D1, D2 and D3 cancel for small tau (D3 ~ -tau^5/20 from tau^4 terms); below tau = 2
 // they come from a fitted polynomial of their series, like the forward's stable terms. The exponentials
 // are recomputed from tau in the reverse sweep instead of being stored; psi entering
 // each segment is recorded by a first forward pass (one float per segment and group).
@@ -84,14 +84,62 @@ __device__ __forceinline__ AdjTerms adj_terms(float tau)
     return r;
 }
 
+// The pair layout of the cell blocks for lanes holding pairs of groups (f32_pairs(VEC)):
+// groups 2j and 2j + 1 of the lane in two float4, (s_a, s_b, a0_a, a0_b) and
+// (a1_a, a1_b, a2_a, a2_b). blk_group reads group k of a lane's blocks in either layout.
+template <int VEC>
+__device__ __forceinline__ float4 blk_group(const float4 (&b)[VEC], int k)
+{
+    if constexpr (f32_pairs(VEC)) {
+        const float4 u = b[k & ~1], v = b[k | 1];
+        return (k & 1) ? make_float4(u.y, u.w, v.y, v.w) : make_float4(u.x, u.z, v.x, v.z);
+    } else {
+        return b[k];
+    }
+}
+
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
 // psi' of one segment, for the recording pass and the chunk maps: the forward sweep's
 // arithmetic (one ex2.approx for p, e = 1 - p). psi only needs the forward's FP32
 // accuracy, which the plain exponential meets; the cancelling derivative terms of the
-// reverse pass come from their series (adj_terms). Also returns p and e/s.
+// reverse pass come from their series (adj_terms). Also returns p and e/s. With pairs of
+// groups (f32_pairs(VEC)) b holds them in the pair layout and the packed FP32 form runs
+// (fma/mul/add .rn.f32x2: one instruction, two groups): every packed operation stands
+// for the same scalar operation, with 1 - x and a - b written fma(x, -1, 1) and
+// fma(b, -1, a), which round once to the same value, so both forms give identical bits.
 template <int VEC>
 __device__ __forceinline__ void advance(const float4 (&b)[VEC], float ds, Vec<VEC> &psi,
                                         Vec<VEC> &pv, Vec<VEC> &e1v)
 {
+    if constexpr (f32_pairs(VEC)) {
+#pragma unroll
+        for (int k = 0; k < VEC; k += 2) {
+            const float2 s = make_float2(b[k].x, b[k].y), a0 = make_float2(b[k].z, b[k].w);
+            const float2 a1 = make_float2(b[k + 1].x, b[k + 1].y);
+            const float2 a2 = make_float2(b[k + 1].z, b[k + 1].w);
+            const float2 tau = __fmul2_rn(s, dup2(ds));
+            const float2 m = __fmul2_rn(tau, dup2(-1.44269504088896341f));
+            const float2 p = make_float2(ex2_approx(m.x), ex2_approx(m.y));
+            const float2 e = __ffma2_rn(p, dup2(-1.0f), dup2(1.0f));
+            const float2 tme = __ffma2_rn(e, dup2(-1.0f), tau);
+            const float2 rs = make_float2(rcp_approx(s.x), rcp_approx(s.y));
+            const float2 rs2 = __fmul2_rn(rs, rs);
+            const float2 e1 = __fmul2_rn(e, rs), t2 = __fmul2_rn(tme, rs2);
+            const float2 reuse = __ffma2_rn(__fadd2_rn(e1, e1), rs2,
+                                            __fmul2_rn(tau, __fadd2_rn(tau, dup2(-2.0f))));
+            float2 pn = __ffma2_rn(a1, t2, __fmul2_rn(a0, e1));
+            pn = __ffma2_rn(a2, reuse, pn);
+            const float2 np = __ffma2_rn(make_float2(psi.v[k], psi.v[k + 1]), p, pn);
+            psi.v[k] = np.x;
+            psi.v[k + 1] = np.y;
+            pv.v[k] = p.x;
+            pv.v[k + 1] = p.y;
+            e1v.v[k] = e1.x;
+            e1v.v[k + 1] = e1.y;
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < VEC; k++) {
         const float s = b[k].x, a0 = b[k].y, a1 = b[k].z, a2 = b[k].w;
@@ -205,11 +253,12 @@ struct RevSeg {
 // L consecutive 16-byte slots, whole 32-byte sectors, where slots in group order would
 // leave every sector half-covered by each of two reductions (twice the L2 reduction
 // traffic, which bounds the reverse pass).
-__device__ __forceinline__ int grad_slot(int g, int vec, int Gs)
+// grad_of returns group g's (dL/ds, dL/da0, dL/da1, dL/da2) from a cell's row of slots.
+__device__ __forceinline__ float4 grad_of(const float4 *row, int g, int vec, int Gs)
 {
     const int b = g / (32 * vec) * (32 * vec), w = g - b;
     const int L = (Gs - b) / vec < 32 ? (Gs - b) / vec : 32;
-    return b + L * (w % vec) + w / vec;
+    return row[b + L * (w % vec) + w / vec];
 }
 __device__ __forceinline__ void red4_if(float4 *p, const float4 &g, int cell, int lim)
 {
@@ -235,7 +284,8 @@ __device__ __forceinline__ void reverse_segment(const AdjParams &A, const RevSeg
 {
 #pragma unroll
     for (int q = 0; q < VEC; q++) {
-        const float s = sg.b[q].x, a0 = sg.b[q].y, a1 = sg.b[q].z, a2 = sg.b[q].w;
+        const float4 bq = blk_group<VEC>(sg.b, q);
+        const float s = bq.x, a0 = bq.y, a1 = bq.z, a2 = bq.w;
         const float d = sg.d;
         const float ps = sg.psi.v[q], la = lam.v[q], W = A.fw.weight * sg.w.v[q];
         const float tau = s * d;
@@ -351,7 +401,7 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
         const int gl = act ? g0 : 0;
         const int lim = act ? nullc : 0;
         const float4 *bb = static_cast<const float4 *>(P.blk) + gl;
-        // this lane's gradient slots: chunk base + lane, then every L slots (grad_slot)
+        // this lane's gradient slots: chunk base + lane, then every L slots (grad_of)
         const int cb0 = g0 - lane * VEC;
         const int gstride = (Gs - cb0) / VEC < 32 ? (Gs - cb0) / VEC : 32;
         float4 *gb = A.gblk + cb0 + lane;
@@ -584,9 +634,9 @@ __global__ void adj_finish_kernel(const float4 *__restrict__ gblk, float *__rest
         const int64_t r = k / Gs;
         const int g = (int)(k - r * Gs);
         if (g >= G) continue;
-        const float4 *cb = gblk + r * I * Gs + grad_slot(g, vec, Gs);
+        const float4 *cb = gblk + r * I * Gs;
         float ds = 0.0f;
-        for (int i = 0; i < I; i++) ds += cb[(int64_t)i * Gs].x;
+        for (int i = 0; i < I; i++) ds += grad_of(cb + (int64_t)i * Gs, g, vec, Gs).x;
         d_sigT[r * Gs + g] = ds;
         // source interval y of region r: every cell i with |i - y| <= 1 whose fit uses it
         for (int y = 0; y < I; y++) {
@@ -595,7 +645,7 @@ __global__ void adj_finish_kernel(const float4 *__restrict__ gblk, float *__rest
                 if (i < 0 || i >= I) continue;
                 const int type = i == 0 ? 0 : (i == I - 1 ? 2 : 1);
                 const int m = y - i + 1;
-                const float4 gq = cb[(int64_t)i * Gs];
+                const float4 gq = grad_of(cb + (int64_t)i * Gs, g, vec, Gs);
                 const float dq[3] = {gq.y, gq.z * mu, gq.w * mu2};
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++) acc = fmaf(jac.a[(type * 3 + kk) * 3 + m], dq[kk], acc);

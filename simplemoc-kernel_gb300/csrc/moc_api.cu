@@ -1287,7 +1287,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t h, const moc_problem_t *p, const moc
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[0], st));
     MOC_CUDA(h, moc::launch_prep_block(p->sigT, p->source, h->blk, p->n_regions,
                                        p->n_intervals, p->group_stride, o->dz, o->zin, o->mu,
-                                       o->mu2, st, true));
+                                       o->mu2, st, true, moc::f32_pairs(vec)));
     MOC_CUDA(h, cudaMemsetAsync(h->gblk, 0, nff * sizeof(float4), st));
     if (prof) MOC_CUDA(h, cudaEventRecord(h->ev[1], st));
     int launches = 1;
