@@ -212,11 +212,17 @@ moc_status_t moc_attenuate_fwd_compact(moc_handle_t handle, const moc_problem_t 
                                        const moc_fwd_opts_t *opts, void *stream);
 
 /*
- * Same sweep, with every pointer of `problem` in HOST memory: the call copies the
- * inputs to device memory held by the handle, sweeps, copies psi and fine_flux back,
- * and returns when the host arrays hold the results. This is the drop-in for a host
- * program that calls run_kernel(I, S, table) on host arrays (src/cpu/main.c:46).
- * Page-locked host memory makes the copies faster but is not required.
+ * Same sweep, with every pointer of `problem` in HOST memory; returns when the host
+ * arrays hold the results. This is the drop-in for a host program that calls
+ * run_kernel(I, S, table) on host arrays (src/cpu/main.c:46). Page-locked arrays mapped
+ * into the device's address space (cudaHostAlloc, cudaHostRegister, pinned torch tensors)
+ * are used in place: the sweep reads the offsets, descriptors and psi over the host link
+ * and writes psi back there; sigT and source are copied up first; the tallies are
+ * reduced on the device and added into fine_flux in place (a fine_flux that is not
+ * mapped is copied up before the sweep and back after it). Other host arrays, and every
+ * array in checked mode, are copied to device memory held by the handle (large problems
+ * in a pipeline of parts) and the results copied back. Page-locked memory is not
+ * required.
  */
 moc_status_t moc_attenuate_fwd_host(moc_handle_t handle, const moc_problem_t *problem,
                                     const moc_fwd_opts_t *opts);
