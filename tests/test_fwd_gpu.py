@@ -179,10 +179,11 @@ def pinned_copy(hp):
     ("adjoint_2M_g64", dict(tracks=50_000)),
 ])
 def test_host_entry_point_reads_pinned_arrays_in_place(handle, name, kw):
-    """Pinned host arrays are swept in place (descriptors, offsets, tables and psi read and
-    psi written over the host link, the tallies on the device): psi equals the device entry
-    point's bit for bit, both outputs are inside the FP64 tolerance, and a bad segment is
-    still reported."""
+    """Pinned host arrays are swept in place (descriptors, offsets and psi read and psi
+    written over the host link, the tables copied up, the tallies reduced on the device
+    and added into fine_flux in place): psi equals the device entry point's bit for bit,
+    both outputs are inside the FP64 tolerance, and a bad segment is still reported. A
+    pageable fine_flux beside pinned inputs is copied up and back instead."""
     hp = mocatt.generate(mocatt.WORKLOADS[name].with_(**kw))
     psi_d, ff_d = run_gpu(handle, hp)
     q, keep = pinned_copy(hp)
@@ -190,6 +191,11 @@ def test_host_entry_point_reads_pinned_arrays_in_place(handle, name, kw):
     assert np.array_equal(q.psi, psi_d)
     ref = oracle.fwd_fp64(hp)
     parity.check_plain(q.psi, q.fine_flux, ref, hp.G)
+    c, keep_c = pinned_copy(hp)
+    c.fine_flux = np.array(hp.fine_flux, copy=True)  # pageable
+    handle.fwd_host(c)
+    assert np.array_equal(c.psi, psi_d)
+    parity.check_plain(c.psi, c.fine_flux, ref, hp.G)
     b, keep_b = pinned_copy(hp)
     b.seg_region[hp.S - 3] = hp.R + 1
     with pytest.raises(mocatt.MocError):
