@@ -468,31 +468,52 @@ def gpu_arm(args, workload):
     if ws == 1 and args.exp == "full" and args.precision == "fp32" and not args.no_extra:
         # the other plain-form lines: the table exp mode on this workload, and the
         # reference's CPU-sized problem (1M segments x 64 groups)
-        line["table"] = plain_timing(h, dp, hp, mocatt.default_opts(
-            profile=1, exp_mode=mocatt.MOC_EXP_TABLE, table_points=args.table_points,
-            table_max=10.0), args.steps, flush, stream)
-        line["table"].update(workload=workload.name, exp_mode="table",
-                             table_points=args.table_points, table_max=10.0)
-        small = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"])
-        sdp = mocatt.DeviceProblem(small, dev)
-        line["sweep_1M_g64"] = plain_timing(h, sdp, small, mocatt.default_opts(profile=1),
-                                            args.steps, flush, stream)
-        line["sweep_1M_g64"].update(workload="sweep_1M_g64", exp_mode="full")
-        del sdp
+        def table_line():
+            r = plain_timing(h, dp, hp, mocatt.default_opts(
+                profile=1, exp_mode=mocatt.MOC_EXP_TABLE, table_points=args.table_points,
+                table_max=10.0), args.steps, flush, stream)
+            r.update(workload=workload.name, exp_mode="table", table_points=args.table_points,
+                     table_max=10.0)
+            return r
+
+        def small_line():
+            small = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"])
+            sdp = mocatt.DeviceProblem(small, dev)
+            r = plain_timing(h, sdp, small, mocatt.default_opts(profile=1), args.steps, flush,
+                             stream)
+            r.update(workload="sweep_1M_g64", exp_mode="full")
+            return r
+
+        optional_section(line, "table", table_line)
+        optional_section(line, "sweep_1M_g64", small_line)
     if not args.no_forms and ws == 1:
-        line["forms"] = forms_section(h, dp, hp, statistics.mean(sweep_ms))
+        optional_section(line, "forms",
+                         lambda: forms_section(h, dp, hp, statistics.mean(sweep_ms)))
     if not args.no_tracks and ws == 1:
-        line["tracks"] = tracks_section(h)
-        line["transport"] = transport_section(h)
+        optional_section(line, "tracks", lambda: tracks_section(h))
+        optional_section(line, "transport", lambda: transport_section(h))
     if not args.no_cpu_baseline and ws == 1:
-        r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
-                         args.table_points if args.exp == "table" else 0)
-        line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": r["cores"],
-                                "kind": "port", "sample": r["sample"],
-                                "compiler": r["compiler"]}
+        def cpu_line():
+            r = cpu_baseline(workload, args.cpu_sample_tracks, 3, 1,
+                             args.table_points if args.exp == "table" else 0)
+            return {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+                    "sample": r["sample"], "compiler": r["compiler"]}
+
+        optional_section(line, "cpu_baseline", cpu_line)
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def optional_section(line: dict, key: str, fn) -> None:
+    """line[key] = fn(); a section beside the headline that fails records its error there
+    (and on stderr) instead of costing the whole line."""
+    try:
+        line[key] = fn()
+    except Exception as e:  # noqa: BLE001 - any failure of an optional section
+        msg = f"{type(e).__name__}: {e}"
+        print(f"warning: bench section {key} failed: {msg}", file=sys.stderr)
+        line[key] = {"error": msg[:400]}
 
 
 def _time_fwd(h, dp, opts, reps=3):
