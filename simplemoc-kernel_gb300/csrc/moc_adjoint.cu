@@ -456,7 +456,10 @@ __global__ void __launch_bounds__(256) adj_reverse_kernel(const AdjParams A)
 // Maps of every chunk of a split track, per group: psi_out = a psi_in + b (forward) and
 // lambda_in = a lambda_out + c (reverse), with a the product of the chunk's p and
 // c = sum_j (product of p before segment j) W_j e_j / s_j, the chunk's lambda sources
-// carried to its start. The arithmetic is the recording pass's (advance).
+// carried to its start. The arithmetic is the recording pass's (advance); the segment loop
+// is the recording pass's branch-free windowed pair loop (segments past the chunk's end
+// decode to the null cell, an exact no-op with W = 0). Map items are full chunks of equal
+// length, so a static warp-strided assignment balances them without a queue atomic.
 template <int VEC>
 __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
 {
@@ -466,13 +469,12 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
     n_maps = n_maps < P.rec_cap ? n_maps : P.rec_cap;
     const int64_t n_items = n_maps * P.n_chunks;
     const int64_t n_units = adj_units(P);
-    for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(P.counter, 1ULL);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= (unsigned long long)n_items) break;
-        const int ch = (int)((int64_t)item / n_maps);
-        const int64_t m = (int64_t)item - (int64_t)ch * n_maps;
+    const int nullc = P.null_cell;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t item = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+         item < n_items; item += nw) {
+        const int ch = (int)(item / n_maps);
+        const int64_t m = item - (int64_t)ch * n_maps;
         const int64_t q = P.map_list[m];
         if ((uint64_t)q >= (uint64_t)n_units) continue;
         AdjItem it;
@@ -482,7 +484,9 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
         const int nvalid = P.G - g0;
         const bool act = nvalid > 0;
         const int Gs = P.Gs;
-        const float4 *bb = static_cast<const float4 *>(P.blk) + g0;
+        // idle lanes (groups past G) read group 0 and store nothing
+        const int gl = act ? g0 : 0;
+        const float4 *bb = static_cast<const float4 *>(P.blk) + gl;
         Vec<VEC> ma, mb, mc;
 #pragma unroll
         for (int k = 0; k < VEC; k++) {
@@ -490,62 +494,52 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
             mb.v[k] = 0.0f;
             mc.v[k] = 0.0f;
         }
+        // a segment's blocks and loss weights (none for the null cell)
+        auto fetch = [&](int c, float4 (&b)[VEC], Vec<VEC> &wv) {
+            load4<VEC>(bb + c * Gs, b);
+            wv = ld_psi<VEC>(A.w + (c < nullc ? c : 0) * Gs + gl, VEC);
+            if (c >= nullc) {
+#pragma unroll
+                for (int k = 0; k < VEC; k++) wv.v[k] = 0.0f;
+            }
+        };
+        auto step = [&](const float4 (&b)[VEC], float d, const Vec<VEC> &wv) {
+            Vec<VEC> pv, e1v;
+            advance<VEC>(b, d, mb, pv, e1v);
+#pragma unroll
+            for (int k = 0; k < VEC; k++) {
+                mc.v[k] = fmaf(ma.v[k], P.weight * wv.v[k] * e1v.v[k], mc.v[k]);
+                ma.v[k] *= pv.v[k];
+            }
+        };
         int64_t wb = beg;
         int cA, cB;
         float dA, dB;
-        decode(P, wb + lane, beg, end, -1, cA, dA);
-        decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
-        auto desc = [&](int64_t j, int &c, float &d) {
-            int k = (int)(j - wb);
-            if (k >= 32) {
-                cA = cB;
-                dA = dB;
-                wb += 32;
-                k -= 32;
-                decode(P, wb + 32 + lane, beg, end, -1, cB, dB);
+        decode(P, wb + lane, beg, end, nullc, cA, dA);
+        decode(P, wb + 32 + lane, beg, end, nullc, cB, dB);
+        float4 b0[VEC], b1[VEC];
+        Vec<VEC> w0, w1;
+        int c0 = __shfl_sync(FULL, cA, 0), c1;
+        float d0 = __shfl_sync(FULL, dA, 0), d1;
+        fetch(c0, b0, w0);
+        for (; wb < end; wb += 32) {
+            const int nk = end - wb < 32 ? (int)(end - wb) : 32;
+            for (int k = 0; k < nk; k += 2) {
+                c1 = __shfl_sync(FULL, cA, k + 1);
+                d1 = __shfl_sync(FULL, dA, k + 1);
+                fetch(c1, b1, w1);
+                step(b0, d0, w0);
+                const int kn = k + 2;
+                const int cs = kn < 32 ? cA : cB;
+                const float dsn = kn < 32 ? dA : dB;
+                c0 = __shfl_sync(FULL, cs, kn & 31);
+                d0 = __shfl_sync(FULL, dsn, kn & 31);
+                fetch(c0, b0, w0);
+                step(b1, d1, w1);
             }
-            c = __shfl_sync(FULL, cA, k);
-            d = __shfl_sync(FULL, dA, k);
-        };
-        int c0 = -1;
-        float d0 = 0.0f;
-        float4 b0[VEC];
-        Vec<VEC> w0;
-        if (beg < end) {
-            desc(beg, c0, d0);
-            if (c0 >= 0 && act) {
-                load4<VEC>(bb + c0 * Gs, b0);
-                w0 = ld_psi<VEC>(A.w + c0 * Gs + g0, nvalid);
-            }
-        }
-        for (int64_t j = beg; j < end; j++) {
-            int c1 = -1;
-            float d1 = 0.0f;
-            float4 b1[VEC];
-            Vec<VEC> w1;
-            if (j + 1 < end) {
-                desc(j + 1, c1, d1);
-                if (c1 >= 0 && act) {
-                    load4<VEC>(bb + c1 * Gs, b1);
-                    w1 = ld_psi<VEC>(A.w + c1 * Gs + g0, nvalid);
-                }
-            }
-            if (act && c0 >= 0) {
-                // b is the map of psi from 0 (advance), c gathers W e/s carried back to the
-                // chunk's start by the product of p so far (a before this segment)
-                Vec<VEC> pv, e1v;
-                advance<VEC>(b0, d0, mb, pv, e1v);
-#pragma unroll
-                for (int k = 0; k < VEC; k++) {
-                    mc.v[k] = fmaf(ma.v[k], P.weight * w0.v[k] * e1v.v[k], mc.v[k]);
-                    ma.v[k] *= pv.v[k];
-                }
-            }
-            c0 = c1;
-            d0 = d1;
-#pragma unroll
-            for (int v = 0; v < VEC; v++) b0[v] = b1[v];
-            w0 = w1;
+            cA = cB;
+            dA = dB;
+            decode(P, wb + 64 + lane, beg, end, nullc, cB, dB);
         }
         if (act) {
             st_psi<VEC>(P.map_a + q * Gs + g0, ma, nvalid);
