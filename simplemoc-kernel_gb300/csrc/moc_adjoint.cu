@@ -549,11 +549,13 @@ __global__ void __launch_bounds__(256) adj_map_kernel(const AdjParams A)
     }
 }
 
-// psi entering and lambda leaving every chunk of the split tracks. One warp per (track,
-// 32-group slice, direction), lanes over groups: psi_0 = psi_in, psi_{k+1} = a_k psi_k +
-// b_k forwards; lambda leaving the last chunk = dL/dpsi_out, lambda leaving chunk k-1 =
-// a_k lambda_k + c_k backwards. The maps of 8 chunks are loaded ahead of their 8
-// dependent FMAs.
+// psi entering and lambda leaving every chunk of the split tracks: one warp per (split
+// track, 32-group slice, direction), its lanes over the slice's groups: psi_0 = psi_in,
+// psi_{k+1} = a_k psi_k + b_k forwards; lambda leaving the last chunk = dL/dpsi_out,
+// lambda leaving chunk k-1 = a_k lambda_k + c_k backwards. The maps of 8 chunks are
+// loaded ahead of their 8 dependent FMAs. The split tracks are found from whichever list
+// is shorter: the tracks (by_track), or the map items, which hold every chunk of a split
+// track and so its first chunk once.
 __global__ void adj_start_kernel(const AdjParams A)
 {
     const SweepParams &P = A.fw;
@@ -566,14 +568,28 @@ __global__ void adj_start_kernel(const AdjParams A)
     float *__restrict__ lam_end = A.lam_end;
     constexpr int NB = 8;
     const int nsl = (P.G + 31) / 32;
-    const int64_t units = (int64_t)P.T * nsl * 2;
+    int64_t n_map = *P.n_map;
+    n_map = n_map < P.rec_cap ? n_map : P.rec_cap;
+    const bool by_track = n_map > P.T;
+    const int64_t units = (by_track ? (int64_t)P.T : n_map) * nsl * 2;
     for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units;
          u += nwarps) {
-        const int64_t t = u / (2 * nsl);
-        const int rest = (int)(u - t * 2 * nsl);
+        const int64_t m = u / (2 * nsl);
+        const int rest = (int)(u - m * 2 * nsl);
         const int sl = rest >> 1, dir = rest & 1;
-        const int64_t b = A.base[t];
-        if (b >= P.rec_cap) continue;
+        int64_t t, b;
+        if (by_track) {
+            t = m;
+            b = A.base[t];
+            if (b >= P.rec_cap) continue;
+        } else {
+            const int64_t q = P.map_list[m];
+            if ((uint64_t)q >= (uint64_t)P.rec_cap) continue;
+            const int4 r = P.rec[q];
+            if (!(r.z & CHUNK_FIRST) || (unsigned)r.w >= (unsigned)P.T) continue;
+            t = r.w;
+            b = q;
+        }
         const int64_t e = A.base[t + 1] < P.rec_cap ? A.base[t + 1] : P.rec_cap;
         const int64_t nq = e - b;
         const int g = sl * 32 + lane;

@@ -175,10 +175,27 @@ __global__ void __launch_bounds__(SCAN_BLOCK) split_records_kernel(const SweepPa
     if (dropped) atomicOr(P.err, DEVERR_OFFSETS);
 }
 
-// psi entering each chunk of every split track. The map list holds every non-last chunk,
-// so each split track's first chunk appears in it once: one warp per map item, and the
-// warp whose item is a first chunk walks that track with its lanes over groups (an empty
-// list - no cut track - costs one load per warp).
+// The split tracks, for the start passes: track u's first record, or -1 for a track that
+// is not cut. They are found from whichever list is shorter, the tracks (by_track) or the
+// map items (every split track's first chunk is one of them, once).
+__device__ __forceinline__ int64_t split_track_of(const SweepParams &P, const SplitWork &W,
+                                                  bool by_track, int64_t u, int64_t &t)
+{
+    if (by_track) {
+        t = u;
+        const int64_t b = W.base[t];
+        return b < W.cap ? b : -1;
+    }
+    const int64_t q = W.map_list[u];
+    if ((uint64_t)q >= (uint64_t)W.cap) return -1;
+    const int4 r = W.rec[q];
+    if (!(r.z & CHUNK_FIRST) || (unsigned)r.w >= (unsigned)P.T) return -1;
+    t = r.w;
+    return q;
+}
+
+// psi entering each chunk of every split track: one warp per (split track, 32-group
+// slice), its lanes over the slice's groups (split_track_of finds the tracks).
 __global__ void split_start_kernel(const SweepParams P, const SplitWork W)
 {
     const int lane = threadIdx.x & 31;
@@ -188,20 +205,22 @@ __global__ void split_start_kernel(const SweepParams P, const SplitWork W)
     float *__restrict__ start = P.start;
     int64_t n_map = *W.n_map;
     n_map = n_map < W.cap ? n_map : W.cap;
-    for (int64_t m = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; m < n_map;
-         m += nwarps) {
-        const int64_t q = W.map_list[m];
-        if ((uint64_t)q >= (uint64_t)W.cap) continue;
-        const int4 r = W.rec[q];
-        if (!(r.z & CHUNK_FIRST) || (unsigned)r.w >= (unsigned)P.T) continue;
-        const int64_t t = r.w;
-        const int64_t b = q;
+    const bool by_track = n_map > P.T;
+    const int nsl = (P.G + 31) / 32;
+    const int64_t units = (by_track ? (int64_t)P.T : n_map) * nsl;
+    for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units;
+         u += nwarps) {
+        const int64_t m = u / nsl;
+        const int g = (int)(u - m * nsl) * 32 + lane;
+        int64_t t = 0;
+        const int64_t b = split_track_of(P, W, by_track, m, t);
+        if (b < 0) continue;
         const int64_t e = W.base[t + 1] < W.cap ? W.base[t + 1] : W.cap;
         const int64_t nq = e - b;
-        for (int g = lane; g < P.G; g += 32) {
+        if (nq >= 2 && g < P.G) {
             float psi = P.psi[t * P.Gs + g];
-            // the maps of 8 chunks are loaded before their 8 dependent FMAs, so the chain
-            // waits for memory once per 8 chunks, not once per chunk
+            // the maps of SCAN_BATCH chunks are loaded before their dependent FMAs, so the
+            // chain waits for memory once per batch, not once per chunk
             for (int64_t c0 = 0; c0 < nq; c0 += SCAN_BATCH) {
                 float av[SCAN_BATCH], bv[SCAN_BATCH];
 #pragma unroll
