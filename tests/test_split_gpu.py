@@ -88,6 +88,16 @@ def test_auto_chunk_cuts_long_tracks_of_small_problems(handle, long_tracks):
     parity.check_plain(p_auto, f_auto, ref, hp.G)
 
 
+def test_auto_chunk_floor_at_a_sixteenth_of_the_mean_track(handle):
+    """1,000 equal tracks of 1,000 segments (1M x 64): the problem's size alone would give
+    C = 32, but the chunk length is at least a sixteenth of the mean track length (rounded
+    up to a power of two), 64 here - the same psi as an explicit C = 64, bit for bit."""
+    hp = mocatt.generate(mocatt.WORKLOADS["sweep_1M_g64"])
+    p_auto, _ = run(handle, hp, mocatt.default_opts())
+    p_64, _ = run(handle, hp, mocatt.default_opts(track_chunk=64))
+    assert np.array_equal(p_auto, p_64)
+
+
 def test_split_deterministic(handle, long_tracks):
     hp, _ = long_tracks
     p1, _ = run(handle, hp, mocatt.default_opts(track_chunk=64))
