@@ -672,14 +672,15 @@ def forms_section(h, dp, hp, plain_sweep_ms) -> dict:
     t_plain = _time_fwd(h, dp, plain)
 
     # adjoint: on the bench problem (50M x 128, the size the adjoint's cost target is
-    # stated at) and on the gradient-check workload (5,000 lognormal tracks, ~2M
-    # segments, G = 64)
+    # stated at), on the gradient-check workload (5,000 lognormal tracks, ~2M segments,
+    # G = 64) and on the reference's CPU-sized problem (1M x 64)
     out["adjoint"] = {"sweep_50M_g128": _adjoint_vs_forward(h, dp, plain, t_plain)}
-    ahp = mocatt.generate(mocatt.WORKLOADS["adjoint_2M_g64"])
-    adp = mocatt.DeviceProblem(ahp)
-    out["adjoint"]["adjoint_2M_g64"] = _adjoint_vs_forward(h, adp, plain,
-                                                           _time_fwd(h, adp, plain))
-    del adp
+    for name in ("adjoint_2M_g64", "sweep_1M_g64"):
+        ahp = mocatt.generate(mocatt.WORKLOADS[name])
+        adp = mocatt.DeviceProblem(ahp)
+        out["adjoint"][name] = _adjoint_vs_forward(h, adp, plain, _time_fwd(h, adp, plain, 7),
+                                                   7)
+        del adp
 
     # batching: three problems (G = 16, 70, 128), one graph-captured launch
     bh = [mocatt.generate(mocatt.WORKLOADS[n])
