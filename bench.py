@@ -250,7 +250,7 @@ def config_of(args, w) -> dict:
                   "exceeds L2", "parallelism": "replicas only (one sweep per GPU)"}
 
 
-def survey_bytes_per_unit(I: int, G: int) -> float:
+def reference_bytes_per_unit(I: int, G: int) -> float:
     """L2 bytes per segment*group of the reference's own access pattern: sigT 4 B, the
     source rows the axial fit reads (two at the first and last interval, three inside:
     4 (2*2 + 3*(I-2)) / I B), the tally 4 B, and an 8-byte descriptor per segment (8/G).
@@ -273,10 +273,10 @@ def sweep_roofline(hp, sweep_ms: float, prep_ms: float, split_ms: float) -> dict
     sweep_s = sweep_ms * 1e-3
     per = l2_bytes_per_unit(hp.I, hp.G)
     layout_b = per["gather"] + per["reduce"]
-    survey_b = survey_bytes_per_unit(hp.I, hp.G)
+    ref_b = reference_bytes_per_unit(hp.I, hp.G)
     roof = {"bound": "l2", "unit": "GB/s",
-            "achieved": survey_b * units / sweep_s / 1e9,
-            "algorithmic_bytes_per_unit": survey_b,
+            "achieved": ref_b * units / sweep_s / 1e9,
+            "algorithmic_bytes_per_unit": ref_b,
             "bytes_model": "the reference's access pattern: sigT + the fit's source rows + "
                            "tally + descriptor (18.46 B per segment*group at 50M x 128)",
             "achieved_layout": layout_b * units / sweep_s / 1e9,
@@ -293,7 +293,7 @@ def sweep_roofline(hp, sweep_ms: float, prep_ms: float, split_ms: float) -> dict
                                f"{peaks.get('clocks', {}).get('sm_mhz')} MHz")
         roof["frac"] = roof["achieved"] / roof["peak"]
         roof["frac_layout"] = roof["achieved_layout"] / roof["peak"]
-        terms["l2"] = survey_b * units / (roof["peak"] * 1e9) * 1e3
+        terms["l2"] = ref_b * units / (roof["peak"] * 1e9) * 1e3
         fp32 = max(peaks.get("fp32_fma_tflops", 0.0), peaks.get("fp32_fma2_tflops", 0.0))
         terms["fp32"] = FP32_OPS_PER_UNIT * units / (fp32 * 1e12 / 2) * 1e3
         terms["mufu"] = MUFU_OPS_PER_UNIT * units / (peaks["mufu_ex2_gops"] * 1e9) * 1e3

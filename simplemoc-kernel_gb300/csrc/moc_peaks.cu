@@ -1,8 +1,8 @@
 // moc_peaks.cu — microbenchmarks for the roofline of the sweep (libmocpeaks.so).
 //
 // The sweep is not bound by HBM or tensor cores but by L2 (row gathers and tally
-// reductions into L2-resident tables) and by FP32/MUFU issue. None of those peaks is in
-// the measured set, so this file measures them on the GPU at hand:
+// reductions into L2-resident tables) and by FP32/MUFU issue. None of those peaks is a
+// plain HBM copy or a bf16 GEMM, so this file measures them on the GPU at hand:
 //   [0] L2 streaming read GB/s   float4 __ldcg over a 64 MiB buffer, many passes
 //   [1] L2 row-gather GB/s       one random 512-byte row per warp from a 96 MiB table
 //                                (the sweep's sigT / coefficient row pattern)
