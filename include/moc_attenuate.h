@@ -316,8 +316,7 @@ moc_status_t moc_attenuate_adj(moc_handle_t handle, const moc_problem_t *problem
  * MOC_ERR_TOO_LARGE.
  *
  * The first call on each device looks up the array's device address (once, with that
- * device current); make that first call before any stream capture. The address is kept
- * for the life of the process: after cudaDeviceReset of a device (which unloads the
+ * device current) and keeps it for the life of the process: after cudaDeviceReset of a device (which unloads the
  * library's device image there) this entry point must not be called on that device
  * again. Every call shares the one array, and it keeps the last call's contents: calls
  * whose kernels overlap on the GPU race on it, so order them on one stream. Every array

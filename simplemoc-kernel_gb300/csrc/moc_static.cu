@@ -14,8 +14,7 @@
 // memory, silently use the wrong memory. So the first call on each device (with that
 // device current) asks the runtime for the array's device address with
 // cudaGetSymbolAddress, checks the result, and caches it; later calls pass the cached
-// address to the kernels. That set-up makes the first call on a device different from
-// the rest, so make the first call on each device before any stream capture.
+// address to the kernels.
 //
 // Every call shares the one array and it keeps the last call's contents: each call
 // clears the work-queue head and error word before its kernels run and rewrites the cell
