@@ -125,8 +125,9 @@ moc_status_t check_problem(const moc_problem_t *p, const moc_fwd_opts_t *o)
         p->group_stride < p->n_groups || p->n_tracks < 0 || p->n_segments < 0)
         return MOC_ERR_INVALID_ARG;
     if (p->group_stride % 4 != 0) return MOC_ERR_UNSUPPORTED;
-    // cell * group_stride is formed in 32-bit arithmetic by the sweep
-    if ((int64_t)p->n_regions * p->n_intervals * p->group_stride > INT32_MAX)
+    // cell * group_stride + group is formed in 32-bit arithmetic by the sweep, for every
+    // cell and the null cell after them
+    if (((int64_t)p->n_regions * p->n_intervals + 1) * p->group_stride > INT32_MAX)
         return MOC_ERR_UNSUPPORTED;
     if (!p->track_offsets || !p->sigT || !p->source || !p->fine_flux) return MOC_ERR_INVALID_ARG;
     if (p->n_tracks > 0 && !p->psi) return MOC_ERR_INVALID_ARG;
@@ -379,7 +380,10 @@ moc_status_t fwd_device(moc_handle_t h, const moc_problem_t *p, const moc_fwd_op
         MOC_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(int32_t),
                                     cudaMemcpyDeviceToHost, st));
         MOC_CUDA(h, cudaStreamSynchronize(st));
-        if (*h->err_host) return MOC_ERR_BAD_INDEX;
+        if (*h->err_host) {
+            MOC_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(int32_t), st));  // reported here
+            return MOC_ERR_BAD_INDEX;
+        }
     }
     if (p->n_tracks == 0) return MOC_OK;
 

@@ -71,3 +71,5 @@ def test_compact_bad_cells_are_reported(handle):
     assert e.value.status == mocatt.MOC_ERR_BAD_INDEX
     np.testing.assert_array_equal(dp2.to_host("psi"), hp.psi)
     assert not dp2.to_host("fine_flux").any()
+    # the refusal was the report: nothing is left for the next synchronisation
+    assert handle.synchronize() == 0

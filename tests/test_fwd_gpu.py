@@ -215,6 +215,7 @@ def test_bad_index_is_skipped_and_reported(handle):
     assert st == mocatt.MOC_ERR_BAD_INDEX
     np.testing.assert_array_equal(dp.to_host("psi"), hp.psi)
     assert not dp.to_host("fine_flux").any()
+    assert handle.synchronize() == 0  # the refusal was the report
     handle.fwd(dp)
     assert handle.synchronize() == mocatt.MOC_ERR_BAD_INDEX
     assert handle.synchronize() == 0  # cleared
