@@ -135,7 +135,8 @@ typedef struct {
     float dz, zin, weight, mu, mu2;
     int32_t checked;              /* 1: bounds-check every segment first (an extra pass)
                                      and return MOC_ERR_BAD_INDEX without touching
-                                     fine_flux or psi                                     */
+                                     fine_flux or psi (that return is the report:
+                                     moc_synchronize has nothing left to report)          */
     int32_t vec;                  /* groups per lane: 0 = auto, else 1, 2 or 4          */
     int32_t warps_per_block;      /* 0 = auto (8; 16 in table mode), else 1..16          */
     int32_t profile;              /* 1: time each kernel of the call with CUDA events on
